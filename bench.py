@@ -1,0 +1,302 @@
+"""Benchmark of the GB300 collide-stream path on the reference's headline workload:
+D2Q9 TRT (magic Λ = 1/4) Poiseuille channel, 4096 x 4096 nodes, bounce-back walls North and
+South, periodic in x, constant body force Fx = 1e-6 (lattice units), τ_s drawn uniformly
+from [0.55, 1.5] with a fixed seed, ρ = 1, u = 0 start.
+
+One benchmark step is one lattice-Boltzmann time step (collide -> stream -> bounce-back) of
+the whole 4096^2 lattice; the default run times 2000 steps, the configuration's run length.
+`value` is MLUPS (million lattice updates per second) with the populations resident in HBM
+(FP64 storage, FP64 arithmetic); `e2e` is the same metric through the C ABI with the host
+arrays copied in and out inside the timed region.  Extra keys report the FP32-deviation
+storage and the CPU baseline (the oracle port on the host cores).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 4096
+Q = 9
+SEED = 20240611
+METRIC = "D2Q9 TRT 4096² MLUPS & %HBM peak: FP64 vs FP32-dev, batched, adjoint"
+BYTES_PER_LU = {"f64": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2}
+
+
+def tau_from_seed():
+    rng = np.random.default_rng(SEED)
+    return float(rng.uniform(0.55, 1.5))
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the fused step kernel from the committed ncu summary."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = float(parts[2])
+                except ValueError:
+                    continue
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for name, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_model(lbm, storage, tau_s):
+    q = lbm.D2Q9()
+    nu = (tau_s - 0.5) / q.speed_of_sound_squared
+    u_max = 0.05
+    problem = lbm.PoiseuilleFlow.fields(1.0, u_max, nu, NX, NY, 1.0, (1.0, 1.0), 1.0)
+    problem.G = 1e-6 / (u_max * problem.delta_t() * problem.viscosity())  # lattice force 1e-6
+    cm = lbm.TRT.fields(tau_s, 0.5 + 0.25 / (tau_s - 0.5), "problem")
+    f0 = lbm.initialize(lbm.ZeroVelocityInitialCondition(), q, problem)
+    model = lbm.LatticeBoltzmannModel(problem, q, collision_model=cm, storage=storage, f0=f0)
+    return problem, model, f0
+
+
+def time_device(torch, model, steps, warmup, dt):
+    """K steps timed with CUDA events on the stream the kernels run on."""
+    stream = torch.cuda.Stream()
+    model.lattice.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        model.lattice.step(warmup, 0, dt)
+        torch.cuda.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        model.lattice.step(steps, warmup, dt)
+        end.record(stream)
+        end.synchronize()
+        torch.cuda.synchronize()
+    launches = model.lattice.last_launch_count()
+    return start.elapsed_time(end) / 1e3, launches
+
+
+def time_e2e(torch, lbm, problem, model, f0, steps, dt):
+    """Upload from pinned host memory, K steps, download to pinned host memory."""
+    stream = torch.cuda.Stream()
+    model.lattice.set_stream(stream.cuda_stream)
+    host_in = torch.from_numpy(f0).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        model.lattice.upload(host_in)
+        model.lattice.step(steps, 0, dt)
+        model.lattice.download(host_out)
+        end.record(stream)
+        end.synchronize()
+    return start.elapsed_time(end) / 1e3, host_in.numel() * 8, host_out.numel() * 8
+
+
+def cpu_baseline(tau_s, budget_s=12.0):
+    """The oracle port (collide -> stream -> bounce-back, OpenMP over x) on the host cores, on
+    a bounded sample of the workload: whole 4096^2 time steps, as many as fit the budget."""
+    from oracle import oracle as O
+    threads = O.max_threads()
+    nu = (tau_s - 0.5) / 3.0
+    p = O.poiseuille_struct(1.0, 0.05, nu, NX, NY, 1.0, (1.0, 1.0), 1.0)
+    sc = O.problem_scalars(p)
+    p.G = 1e-6 / (0.05 * sc["delta_t"] * sc["viscosity"])
+    cm = O.collision("TRT", [tau_s, 0.5 + 0.25 / (tau_s - 0.5)], force=True)
+    bcs = [O.bc("bounce_back", "north", (1, NX), (1, NY)), O.bc("bounce_back", "south", (1, NX), (1, NY))]
+    f = O.initialize(O.INIT_ZERO_VELOCITY, "D2Q9", p)
+    t0 = time.perf_counter()
+    f = O.run("D2Q9", p, cm, bcs, f, 0, 0, dt=sc["delta_t"], nthreads=threads)
+    one = time.perf_counter() - t0
+    n = max(1, min(50, int(budget_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    O.run("D2Q9", p, cm, bcs, f, 1, n, dt=sc["delta_t"], nthreads=threads)
+    el = time.perf_counter() - t0
+    return {"value": NX * NY * n / el / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{n} time steps of the full {NX}x{NY} lattice (after 1 warm-up step), "
+                      f"{threads} OpenMP threads, C++ restatement of the reference loop"}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return 0
+    tau_s = tau_from_seed()
+    from oracle import oracle as O
+    O.build()
+    steps = max(1, args.steps)
+    res = cpu_baseline(tau_s, budget_s=min(120.0, 3.0 + 0.05 * steps))
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "MLUPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": NX * NY / res["value"] / 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "D2Q9 TRT Poiseuille 4096x4096, FP64, CPU oracle port (the reference is Julia, "
+                                   "not runnable on the box)", "nx": NX, "ny": NY, "tau_s": tau_s},
+            "cpu_baseline": res,
+            "e2e": {"value": res["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--storage", default="f64", choices=["f64", "f32dev", "f16dev"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.warmup < 3:
+        args.warmup = 3
+
+    import torch
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    lbm = __graft_entry__.load_package()
+    lbm._native.lib()
+    tau_s = tau_from_seed()
+
+    problem, model, f0 = build_model(lbm, args.storage, tau_s)
+    dt = problem.delta_t()
+    with ClockSampler(local) as clk:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        seconds, launches = time_device(torch, model, args.steps, args.warmup, dt)
+    clocks = clk.summary()
+    if world > 1:
+        t = torch.tensor([seconds], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        seconds = float(t.item())
+    lu = NX * NY * args.steps
+    mlups = lu / seconds / 1e6 * world
+    per_launch = seconds / max(1, args.steps)
+    bytes_lu = BYTES_PER_LU[args.storage]
+    pk = peaks()
+    peak_gbs = pk["hbm_gbs"] if pk else 6800.0
+    achieved_gbs = bytes_lu * NX * NY / per_launch / 1e9
+    traffic = profiled_traffic().get(f"step_{args.storage}")
+
+    e2e_s, h2d, d2h = time_e2e(torch, lbm, problem, model, f0, args.steps, dt)
+    e2e = {"value": NX * NY * args.steps / e2e_s / 1e6 * world, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+    model.close()
+
+    extra = {}
+    if args.storage == "f64" and rank == 0:
+        _, m32, _ = build_model(lbm, "f32dev", tau_s)
+        s32, _ = time_device(torch, m32, args.steps, args.warmup, dt)
+        m32.close()
+        extra["f32dev"] = {"value": NX * NY * args.steps / s32 / 1e6, "unit": "MLUPS",
+                           "speedup_vs_f64": seconds / s32,
+                           "roofline_frac": BYTES_PER_LU["f32dev"] * NX * NY / (s32 / args.steps) / 1e9 / peak_gbs}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(tau_s)
+    if rank == 0:
+        line = {"metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": seconds / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": args.storage, "data": "synthetic",
+                "config": {"workload": "D2Q9 TRT Poiseuille channel 4096x4096, bounce-back N/S, Fx=1e-6, "
+                                       "u=0 start (one step = one time step of the whole lattice)",
+                           "nx": NX, "ny": NY, "tau_s": tau_s, "tau_a": 0.5 + 0.25 / (tau_s - 0.5),
+                           "storage": args.storage, "parallelism": f"replicas{world}",
+                           "l2": "inputs larger than L2 (two population arrays of "
+                                 f"{NX * NY * Q * bytes_lu // (2 * Q) / 1e9:.2f} GB)"},
+                "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                             "frac": achieved_gbs / peak_gbs, "traffic": traffic,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6.8 TB/s",
+                             "bytes_per_lu": bytes_lu, "kernel": "step_kernel<D2Q9,TRT,fused>"},
+                "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu}
+        line.update(extra)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,205 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300-native lattice-Boltzmann collide-stream library
+ * (liblbm_gb300.so, hand-written CUDA for sm_103a).
+ *
+ * The library replaces the per-step hot path of LatticeBoltzmann.jl:
+ *
+ *   simulate(model, time)            src/lattice_boltzmann_model.jl:60-77
+ *     collide!(model; time)          src/lattice_boltzmann_model.jl:84-92 -> collide!(cm, q, f_in, f_out)
+ *     stream!(model)                 src/lattice_boltzmann_model.jl:94-96 -> stream!(q, f, f_new)
+ *     apply_boundary_conditions!     src/lattice_boltzmann_model.jl:98-106 -> apply!(bcs, q, f_new, f_old)
+ *     next!(model, t)                src/lattice_boltzmann_model.jl:108-110 (the reductions below)
+ *
+ * with one fused pull kernel per time step.  A host binding (Julia `ccall`, Python ctypes)
+ * keeps the reference's problem / initial-condition / processing layer and passes plain data
+ * across this boundary: tables, relaxation times, forces, boundary descriptors and the
+ * distribution array in the reference's own layout f[x, y, i] (column-major Julia array,
+ * i.e. element f[x + nx * (y + ny * i)] with 0-based indices), so `pointer(f::Array{Float64,3})`
+ * passes straight through.
+ *
+ * Conventions
+ *   - Every entry point returns LBM_OK (0) or a negative lbm_status; no exception crosses the
+ *     ABI.  lbm_last_error(ctx) describes the last failure on that context.
+ *   - A context owns all device memory it allocates; host pointers are only read or written
+ *     during the call that receives them.
+ *   - One context is used by one host thread at a time.  Work is issued on the context's
+ *     stream (its own non-blocking stream, or the one given to lbm_set_stream); calls that
+ *     return host data synchronise that stream, lbm_step does not.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_ABI_VERSION 1
+#define LBM_MAX_Q 37
+#define LBM_MAX_BC 8
+
+typedef enum {
+  LBM_OK = 0,
+  LBM_ERR_INVALID = -1,     /* bad argument or descriptor */
+  LBM_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+  LBM_ERR_NOMEM = -3,       /* device or pinned host allocation failed */
+  LBM_ERR_UNSUPPORTED = -4, /* combination not provided (e.g. MRT with FP16 storage) */
+  LBM_ERR_STATE = -5,       /* call out of order (e.g. step before upload) */
+  LBM_ERR_NONFINITE = -6    /* a reduction met NaN / Inf */
+} lbm_status;
+
+/* Velocity sets, in the order of the reference's `Quadratures` tuple (src/quadratures.jl:30-38).
+ * LBM_D2Q21 has 25 velocities, as the reference's D2Q21 (src/quadratures/D2Q21.jl:36-66). */
+typedef enum { LBM_D2Q4 = 0, LBM_D2Q5, LBM_D2Q9, LBM_D2Q13, LBM_D2Q17, LBM_D2Q21, LBM_D2Q37 } lbm_quadrature;
+
+/* Collision operators: SRT  src/collision_models/srt.jl:1-62
+ *                      TRT  src/collision_models/trt.jl:1-97
+ *                      MRT  src/collision_models/mrt.jl:1-118 (regularised / projected)
+ *                      ITERATIVE_INIT  src/collision_models/iterative_initialization.jl:1-60 */
+typedef enum { LBM_SRT = 0, LBM_TRT = 1, LBM_MRT = 2, LBM_ITERATIVE_INIT = 3 } lbm_collision_kind;
+
+/* Device storage of the distributions.  F64 keeps f itself; F32_DEV / F16_DEV keep the
+ * deviation g_i = f_i - w_i and compute in FP32. */
+typedef enum { LBM_STORE_F64 = 0, LBM_STORE_F32_DEV = 1, LBM_STORE_F16_DEV = 2 } lbm_storage;
+
+/* Forcing, applied as the reference does: a velocity shift of the equilibrium, u + τ F
+ * (srt.jl:52-54, trt.jl:76-79, mrt.jl:91-95).
+ *   CONSTANT: (force[0], force[1]) at every node (PoiseuilleFlow, poiseuille.jl:72-82)
+ *   FIELD:    a time-independent lattice force per node, force_field[x + nx*(y + ny*d)]
+ *   SHEAR:    the time-dependent DecayingShearFlow force (decaying_shear_flow.jl:132-147):
+ *             Fx = shear[0] * cos(shear[1] * y - shear[2] * t)
+ *             Fy = shear[3] * cos(shear[4] * x - shear[5] * t)
+ *             with x, y the node coordinates x_coords[x], y_coords[y] and t the step time. */
+typedef enum { LBM_FORCE_NONE = 0, LBM_FORCE_CONSTANT = 1, LBM_FORCE_FIELD = 2, LBM_FORCE_SHEAR = 3 } lbm_force_kind;
+
+/* Boundary conditions (src/boundary_conditions.jl:6-35), applied in list order after the
+ * periodic stream, each reading the post-collision populations of the same node:
+ *   BOUNCE_BACK  src/boundary_conditions/bounce_back.jl:1-72 (all four directions)
+ *   MOVING_WALL  src/boundary_conditions/moving_wall.jl:1-38 (North only; like the
+ *                reference it ignores x_lo..y_hi and covers the whole top wall) */
+typedef enum { LBM_BOUNCE_BACK = 0, LBM_MOVING_WALL = 1 } lbm_bc_kind;
+typedef enum { LBM_NORTH = 0, LBM_EAST = 1, LBM_SOUTH = 2, LBM_WEST = 3 } lbm_direction;
+
+typedef struct {
+  int32_t kind;       /* lbm_bc_kind */
+  int32_t direction;  /* lbm_direction */
+  int32_t x_lo, x_hi; /* the BC's xs, 1-based inclusive (Julia UnitRange) */
+  int32_t y_lo, y_hi; /* the BC's ys, 1-based inclusive */
+  double u[2];        /* MOVING_WALL: wall velocity */
+  double rho;         /* MOVING_WALL: wall density */
+  double T;           /* MOVING_WALL: wall temperature (unused by the reference's rule) */
+} lbm_bc;
+
+typedef struct {
+  int32_t quadrature;             /* lbm_quadrature */
+  double weights[LBM_MAX_Q];      /* w_i as the host quadrature holds them (q.weights) */
+  double speed_of_sound_squared;  /* the reference field of that name, i.e. 1 / c_s^2 */
+  int32_t collision;              /* lbm_collision_kind */
+  double tau[4];                  /* SRT: τ | TRT: τ_symmetric, τ_asymmetric | MRT: τs[1..4] | iterative: τ */
+  int32_t force_kind;             /* lbm_force_kind */
+  double force[2];                /* CONSTANT */
+  const double* force_field;      /* FIELD: host array nx*ny*2, copied at create */
+  double shear[6];                /* SHEAR */
+  const double* x_coords;         /* SHEAR: host array of nx node coordinates */
+  const double* y_coords;         /* SHEAR: host array of ny node coordinates */
+  const double* nonlinear;        /* ITERATIVE_INIT: host array nx*ny*Q of the precomputed
+                                     nonlinear equilibrium term, copied at create */
+  int32_t nbc;                    /* number of boundary conditions, <= LBM_MAX_BC */
+  const lbm_bc* bcs;
+  int64_t nx, ny;                 /* lattice size (Julia size(f, 1), size(f, 2)) */
+  int32_t storage;                /* lbm_storage */
+} lbm_desc;
+
+typedef struct lbm_ctx lbm_ctx;
+
+/* Library identity. */
+int32_t lbm_abi_version(void);
+const char* lbm_status_string(int32_t status);
+
+/* Context lifetime.  Replaces LatticeBoltzmannModel(problem, q; ...) for the data it holds
+ * (src/lattice_boltzmann_model.jl:1-33): the two population arrays, the quadrature, the
+ * collision model and the boundary-condition list. */
+int32_t lbm_create(lbm_ctx** ctx, const lbm_desc* desc);
+void lbm_destroy(lbm_ctx* ctx);
+const char* lbm_last_error(const lbm_ctx* ctx);
+/* Issue the context's work on `stream` (a cudaStream_t); NULL restores the own stream. */
+int32_t lbm_set_stream(lbm_ctx* ctx, void* stream);
+int32_t lbm_synchronize(lbm_ctx* ctx);
+
+/* Populations in and out, in the Julia layout f[x + nx*(y + ny*i)] (FP64).  The state is
+ * the reference's `f_stream` (the array next!(pm, q, f, t) observes). */
+int32_t lbm_upload(lbm_ctx* ctx, const double* f_host);
+int32_t lbm_download(lbm_ctx* ctx, double* f_host);
+int32_t lbm_upload_device(lbm_ctx* ctx, const double* f_device);
+int32_t lbm_download_device(lbm_ctx* ctx, double* f_device);
+
+/* `nsteps` iterations of the reference loop body for t = t0, ..., t0 + nsteps - 1:
+ * collide!(time = t*dt) -> stream! -> apply!(bcs), as simulate(model, time) does
+ * (src/lattice_boltzmann_model.jl:64-67).  Asynchronous on the context's stream. */
+int32_t lbm_step(lbm_ctx* ctx, int64_t nsteps, int64_t t0, double dt);
+
+/* Launch count of the last lbm_step call (kernels issued, for accounting). */
+int64_t lbm_last_launch_count(const lbm_ctx* ctx);
+
+/* ---- reductions for the processing methods (next!) --------------------------------------- */
+
+/* Analytic fields for the error norms, host or device arrays of nx*ny each (Julia layout),
+ * in the dimensionless units the reference compares in. */
+typedef struct {
+  const double* rho;  /* expected density */
+  const double* ux;   /* expected velocity */
+  const double* uy;
+  const double* p;    /* expected pressure */
+  const double* sxx;  /* expected deviatoric stress σ[1,1], σ[2,1], σ[1,2], σ[2,2] */
+  const double* syx;
+  const double* sxy;
+  const double* syy;
+  int32_t on_device;  /* 1: the pointers are device pointers */
+  double tau;         /* τ = (1/c_s²)·ν used by the stress estimate (track_hydrodynamic_errors.jl:148,176) */
+  double u_max;       /* dimensionless_velocity scale (problems.jl:110) */
+  double area;        /* the `opp` cell area of CompareWithAnalyticalSolution (processing_methods.jl:234) */
+} lbm_analytic;
+
+/* Kinds of lbm_reduce:
+ *   TRACK_ERRORS  sums of TrackHydrodynamicErrors.next! (track_hydrodynamic_errors.jl:104-203):
+ *                 out[0..15] = Σ(ρ-ρ*)², Σ|u-u*|², Σ(p-p*)², Σ(σxx-σxx*)², Σ(σxy-σxy*)²,
+ *                 Σ(σyy-σyy*)², Σ(σyx-σyx*)², Σ|u*|², Σσxx*², Σσyy*², Σσxy*², Σσyx*², Σp*²,
+ *                 Σρ, Σρ(ux+uy), Σρ|u|²   (u dimensionless, σ scaled by 1/u_max²)
+ *   COMPARE       sums of CompareWithAnalyticalSolution process! (processing_methods.jl:142-239):
+ *                 out[0..11] = Σρ, Σρ(ux+uy), Σ(ke+T), Σke, ΣT, Σρ*, Σρ*(ux*+uy*), Σ(ke*+T*),
+ *                 Σke*, ΣT*, area·Σ|u-u*|², area·Σ(p-p*)²
+ *   MEAN_VELOCITY Σ ux and the node count (stopping_criteria.jl:34-56): out[0], out[1]
+ *   VELOCITY_CONVERGENCE  Σ|u-u_old|², Σ|u_old|², then u_old := u (stopping_criteria.jl:88-115)
+ *   DENSITY_AT    density of node (ix, iy) = (out[0], out[1]) on entry (density_convergence.jl:6-17)
+ *   CONSERVED     Σρ, Σρux, Σρuy, number of non-finite populations (out[0..3])
+ * Sums are FP64, taken in a fixed order (deterministic across runs). */
+typedef enum {
+  LBM_REDUCE_TRACK_ERRORS = 0,
+  LBM_REDUCE_COMPARE = 1,
+  LBM_REDUCE_MEAN_VELOCITY = 2,
+  LBM_REDUCE_VELOCITY_CONVERGENCE = 3,
+  LBM_REDUCE_DENSITY_AT = 4,
+  LBM_REDUCE_CONSERVED = 5
+} lbm_reduce_kind;
+
+int32_t lbm_reduce(lbm_ctx* ctx, int32_t kind, const lbm_analytic* analytic, double* out);
+
+/* Macroscopic fields of the current state, Julia layout, host arrays of nx*ny
+ * (density / velocity!, src/velocity_distribution_function/moments.jl:1-19).  Any pointer
+ * may be NULL. */
+int32_t lbm_macroscopic(lbm_ctx* ctx, double* rho, double* ux, double* uy);
+
+/* ---- single operators on caller-owned device arrays (FP64, Julia layout) ----------------
+ * The reference's plugin points, for callers that keep their own arrays on the GPU.  They
+ * use the context's quadrature, collision model and BC list; f_in / f_out etc. are device
+ * pointers of nx*ny*Q doubles. */
+int32_t lbm_collide_device(lbm_ctx* ctx, const double* f_in, double* f_out, double time); /* collide!(cm, q, f_in, f_out; time) */
+int32_t lbm_stream_device(lbm_ctx* ctx, const double* f, double* f_new);                   /* stream!(q, f, f_new), periodic */
+int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old);            /* apply!(bcs, q, f_new, f_old) */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

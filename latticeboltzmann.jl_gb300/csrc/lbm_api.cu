@@ -1,0 +1,684 @@
+// lbm_api.cu -- the C ABI of liblbm_gb300.so (declared in include/lbm_gb300.h).
+//
+// A context holds what LatticeBoltzmannModel holds in the reference
+// (src/lattice_boltzmann_model.jl:1-33): the two population arrays (here device buffers in
+// the chosen storage), the quadrature, the collision model and the BC list, plus the stream
+// the work is issued on.  The device state is either the reference's `f_stream` (after an
+// upload) or the post-collision array of the last step, from which `f_stream` is pulled on
+// demand; see lbm_step.cuh.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lbm_ops.cuh"
+
+using namespace lbm;
+
+namespace {
+
+enum Phase { POST_STREAM = 0, POST_COLLIDE = 1 };
+
+typedef cudaError_t (*RunFn)(const OpArgs&);
+const RunFn kRun[7] = {run_op_q4, run_op_q5, run_op_q9, run_op_q13, run_op_q17, run_op_q21, run_op_q37};
+
+struct HostLattice {
+  int Q, R;
+  int cx[LBM_MAX_Q], cy[LBM_MAX_Q], opp[LBM_MAX_Q];
+};
+
+template <class L>
+HostLattice host_lattice() {
+  HostLattice h{};
+  h.Q = L::Q;
+  h.R = L::R;
+  for (int i = 0; i < L::Q; ++i) {
+    h.cx[i] = L::cx(i);
+    h.cy[i] = L::cy(i);
+    h.opp[i] = L::opp(i);
+  }
+  return h;
+}
+
+HostLattice lattice_of(int q) {
+  switch (q) {
+    case LBM_D2Q4: return host_lattice<D2Q4>();
+    case LBM_D2Q5: return host_lattice<D2Q5>();
+    case LBM_D2Q9: return host_lattice<D2Q9>();
+    case LBM_D2Q13: return host_lattice<D2Q13>();
+    case LBM_D2Q17: return host_lattice<D2Q17>();
+    case LBM_D2Q21: return host_lattice<D2Q21>();
+    default: return host_lattice<D2Q37>();
+  }
+}
+
+constexpr int kGraphSteps = 64;                  // steps per captured graph (even: parity kept)
+constexpr size_t kGraphMaxBytes = 256ull << 20;  // capture only lattices whose step is launch-bound
+
+}  // namespace
+
+struct lbm_ctx {
+  int device = 0;
+  int qid = 0, Q = 0, R = 1, storage = 0, coll = 0, force_kind = 0;
+  int64_t nx = 0, ny = 0, n = 0;
+  size_t elem = 8;
+  HostLattice lat{};
+  void* buf[2] = {nullptr, nullptr};
+  int cur = 0;
+  int phase = POST_STREAM;
+  bool have_state = false;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  StepParams<double> pd{};
+  StepParams<float> pf{};
+  ReduceArgs red{};
+  double* d_force = nullptr;
+  double* d_xr = nullptr;
+  double* d_yr = nullptr;
+  void* d_nonlinear = nullptr;
+  double* d_stage = nullptr;    // FP64 planes for deviation-storage transfers
+  double* d_partial = nullptr;  // reduction partial sums
+  int red_blocks = 0;
+  double* d_out = nullptr;
+  double* h_out = nullptr;      // pinned
+  double* d_uold = nullptr;
+  double* d_analytic = nullptr;
+  double* d_macro = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int64_t last_launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(lbm_ctx* c, int status, const std::string& msg) {
+  if (c) c->err = msg;
+  return status;
+}
+
+int cuda_fail(lbm_ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(c, LBM_ERR_CUDA, m);
+}
+
+#define LBM_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+  } while (0)
+
+OpArgs base_args(lbm_ctx* c, int op) {
+  OpArgs a;
+  a.op = op;
+  a.storage = c->storage;
+  a.coll = c->coll;
+  a.pd = &c->pd;
+  a.pf = &c->pf;
+  a.red = &c->red;
+  a.stream = c->stream;
+  return a;
+}
+
+int run(lbm_ctx* c, const OpArgs& a) {
+  cudaError_t e = kRun[c->qid](a);
+  if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
+  c->last_launches += 1;
+  return LBM_OK;
+}
+
+void set_time(lbm_ctx* c, double t) {
+  c->pd.time = t;
+  c->pf.time = t;
+}
+
+int ensure(lbm_ctx* c, double** p, size_t bytes) {
+  if (*p) return LBM_OK;
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(c, LBM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return LBM_OK;
+}
+
+// One time step from the current state into the other buffer.
+int step_once(lbm_ctx* c) {
+  OpArgs a = base_args(c, c->phase == POST_STREAM ? OP_COLLIDE : OP_FUSED);
+  a.src = c->buf[c->cur];
+  a.dst = c->buf[1 - c->cur];
+  int rc = run(c, a);
+  if (rc) return rc;
+  c->cur ^= 1;
+  c->phase = POST_COLLIDE;
+  return LBM_OK;
+}
+
+// f_stream into the other buffer (pull + BCs), leaving the state POST_STREAM.
+int materialise(lbm_ctx* c) {
+  if (c->phase == POST_STREAM) return LBM_OK;
+  OpArgs a = base_args(c, OP_STREAM_BC);
+  a.src = c->buf[c->cur];
+  a.dst = c->buf[1 - c->cur];
+  int rc = run(c, a);
+  if (rc) return rc;
+  c->cur ^= 1;
+  c->phase = POST_STREAM;
+  return LBM_OK;
+}
+
+int graph_for_parity(lbm_ctx* c, int parity, cudaGraphExec_t* out) {
+  if (c->graph[parity]) {
+    *out = c->graph[parity];
+    return LBM_OK;
+  }
+  const int saved_cur = c->cur, saved_phase = c->phase;
+  const int64_t saved_launches = c->last_launches;
+  c->cur = parity;
+  c->phase = POST_COLLIDE;
+  cudaGraph_t g = nullptr;
+  LBM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = LBM_OK;
+  for (int k = 0; k < kGraphSteps && rc == LBM_OK; ++k) rc = step_once(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->cur = saved_cur;
+  c->phase = saved_phase;
+  c->last_launches = saved_launches;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&c->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    c->graph[parity] = nullptr;
+    return cuda_fail(c, e, "cudaGraphInstantiate");
+  }
+  *out = c->graph[parity];
+  return LBM_OK;
+}
+
+void free_graphs(lbm_ctx* c) {
+  for (int k = 0; k < 2; ++k)
+    if (c->graph[k]) {
+      cudaGraphExecDestroy(c->graph[k]);
+      c->graph[k] = nullptr;
+    }
+}
+
+int red_kind_k(int kind) {
+  switch (kind) {
+    case LBM_REDUCE_TRACK_ERRORS: return 16;
+    case LBM_REDUCE_COMPARE: return 12;
+    case LBM_REDUCE_MEAN_VELOCITY: return 2;
+    case LBM_REDUCE_VELOCITY_CONVERGENCE: return 3;
+    case LBM_REDUCE_CONSERVED: return 4;
+    default: return 0;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t lbm_abi_version(void) { return LBM_ABI_VERSION; }
+
+const char* lbm_status_string(int32_t s) {
+  switch (s) {
+    case LBM_OK: return "ok";
+    case LBM_ERR_INVALID: return "invalid argument";
+    case LBM_ERR_CUDA: return "CUDA error";
+    case LBM_ERR_NOMEM: return "out of memory";
+    case LBM_ERR_UNSUPPORTED: return "unsupported";
+    case LBM_ERR_STATE: return "invalid state";
+    case LBM_ERR_NONFINITE: return "non-finite value";
+    default: return "unknown status";
+  }
+}
+
+const char* lbm_last_error(const lbm_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int64_t lbm_last_launch_count(const lbm_ctx* c) { return c ? c->last_launches : 0; }
+
+int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
+  if (!out || !d) return LBM_ERR_INVALID;
+  *out = nullptr;
+  if (d->quadrature < 0 || d->quadrature > 6) return LBM_ERR_INVALID;
+  if (d->nx < 1 || d->ny < 1 || d->nx * d->ny >= (int64_t(1) << 31)) return LBM_ERR_INVALID;
+  if (d->storage < 0 || d->storage > 2) return LBM_ERR_INVALID;
+  if (d->collision < 0 || d->collision > 3) return LBM_ERR_INVALID;
+  if (d->force_kind < 0 || d->force_kind > 3) return LBM_ERR_INVALID;
+  if (d->nbc < 0 || d->nbc > LBM_MAX_BC || (d->nbc > 0 && !d->bcs)) return LBM_ERR_INVALID;
+  if (d->force_kind == LBM_FORCE_FIELD && !d->force_field) return LBM_ERR_INVALID;
+  if (d->force_kind == LBM_FORCE_SHEAR && (!d->x_coords || !d->y_coords)) return LBM_ERR_INVALID;
+  if (d->collision == LBM_ITERATIVE_INIT && !d->nonlinear) return LBM_ERR_INVALID;
+
+  lbm_ctx* c = new lbm_ctx();
+  cudaGetDevice(&c->device);
+  c->qid = d->quadrature;
+  c->lat = lattice_of(c->qid);
+  c->Q = c->lat.Q;
+  c->R = c->lat.R;
+  c->storage = d->storage;
+  c->coll = d->collision;
+  c->force_kind = d->force_kind;
+  c->nx = d->nx;
+  c->ny = d->ny;
+  c->n = d->nx * d->ny;
+  c->elem = d->storage == LBM_STORE_F64 ? 8 : d->storage == LBM_STORE_F32_DEV ? 4 : 2;
+
+  for (int b = 0; b < d->nbc; ++b) {
+    const lbm_bc& s = d->bcs[b];
+    if (s.kind != LBM_BOUNCE_BACK && s.kind != LBM_MOVING_WALL) { delete c; return LBM_ERR_INVALID; }
+    if (s.direction < 0 || s.direction > 3) { delete c; return LBM_ERR_INVALID; }
+    if (s.kind == LBM_MOVING_WALL && s.direction != LBM_NORTH) { delete c; return LBM_ERR_UNSUPPORTED; }
+    const bool xe = s.x_lo > s.x_hi, ye = s.y_lo > s.y_hi;
+    if (s.kind == LBM_BOUNCE_BACK &&
+        ((!xe && (s.x_lo < 1 || s.x_hi > d->nx)) || (!ye && (s.y_lo < 1 || s.y_hi > d->ny)))) {
+      delete c;
+      return LBM_ERR_INVALID;
+    }
+  }
+
+  // parameter blocks (FP64 and FP32 copies; the storage selects one)
+  StepParams<double>& p = c->pd;
+  p.nx = (int)d->nx;
+  p.ny = (int)d->ny;
+  p.n = c->n;
+  for (int dd = -3; dd <= 3; ++dd) {
+    p.dxm[dd + 3] = (int)(((dd % d->nx) + d->nx) % d->nx);
+    p.dym[dd + 3] = (int)(((dd % d->ny) + d->ny) % d->ny);
+  }
+  for (int i = 0; i < LBM_MAX_Q; ++i) p.w[i] = i < c->Q ? d->weights[i] : 0.0;
+  p.cs = d->speed_of_sound_squared;
+  const double* tau = d->tau;
+  if (c->coll == LBM_SRT || c->coll == LBM_ITERATIVE_INIT) {
+    p.om_a = 1 - 1 / tau[0];
+    p.om_b = 1 / tau[0];
+    p.shift = tau[0];
+  } else if (c->coll == LBM_TRT) {
+    p.inv_ts = 1 / tau[0];
+    p.inv_ta = 1 / tau[1];
+    p.shift = tau[1];
+  } else {
+    for (int k = 0; k < 4; ++k) {
+      p.mrt_a[k] = 1 - 1 / tau[k];
+      p.mrt_b[k] = 1 / tau[k];
+    }
+    p.shift = tau[1];
+  }
+  p.force_kind = d->force_kind;
+  p.F[0] = d->force[0];
+  p.F[1] = d->force[1];
+  for (int k = 0; k < 6; ++k) p.shear[k] = d->shear[k];
+  p.nbc = d->nbc;
+  for (int b = 0; b < d->nbc; ++b) {
+    const lbm_bc& s = d->bcs[b];
+    BCDev& t = p.bc[b];
+    t.kind = s.kind;
+    t.dir = s.direction;
+    t.x_lo = s.x_lo - 1;
+    t.x_hi = s.x_hi - 1;
+    t.y_lo = s.y_lo - 1;
+    t.y_hi = s.y_hi - 1;
+    for (int i = 0; i < LBM_MAX_Q; ++i) t.add[i] = 0.0;
+    if (s.kind == LBM_MOVING_WALL) {
+      // a_1 = w_i * cs * dot(ρ_w u_w, c_i), the added term is 2 a_1 (moving_wall.jl:20-33)
+      const double a1x = s.rho * s.u[0], a1y = s.rho * s.u[1];
+      for (int i = 0; i < c->Q; ++i) {
+        const double a1 = d->weights[i] * d->speed_of_sound_squared *
+                          (a1x * (c->lat.cx[i] * 1.0) + a1y * (c->lat.cy[i] * 1.0));
+        t.add[i] = 2 * a1;
+      }
+    }
+  }
+  // FP32 copy
+  StepParams<float>& q = c->pf;
+  q.nx = p.nx;
+  q.ny = p.ny;
+  q.n = p.n;
+  for (int k = 0; k < 7; ++k) {
+    q.dxm[k] = p.dxm[k];
+    q.dym[k] = p.dym[k];
+  }
+  for (int i = 0; i < LBM_MAX_Q; ++i) q.w[i] = (float)p.w[i];
+  q.cs = (float)p.cs;
+  q.om_a = (float)p.om_a;
+  q.om_b = (float)p.om_b;
+  q.inv_ts = (float)p.inv_ts;
+  q.inv_ta = (float)p.inv_ta;
+  q.shift = (float)p.shift;
+  for (int k = 0; k < 4; ++k) {
+    q.mrt_a[k] = (float)p.mrt_a[k];
+    q.mrt_b[k] = (float)p.mrt_b[k];
+  }
+  q.force_kind = p.force_kind;
+  q.F[0] = (float)p.F[0];
+  q.F[1] = (float)p.F[1];
+  for (int k = 0; k < 6; ++k) q.shear[k] = p.shear[k];
+  q.nbc = p.nbc;
+  for (int b = 0; b < p.nbc; ++b) q.bc[b] = p.bc[b];
+
+  // reduction constants
+  for (int i = 0; i < LBM_MAX_Q; ++i) c->red.w[i] = p.w[i];
+  c->red.cs = p.cs;
+  c->red.q_low_order = (c->qid == LBM_D2Q4 || c->qid == LBM_D2Q5) ? 1 : 0;
+
+  cudaError_t e;
+  const size_t bytes = (size_t)c->n * c->Q * c->elem;
+  for (int k = 0; k < 2; ++k) {
+    e = cudaMalloc(&c->buf[k], bytes);
+    if (e != cudaSuccess) {
+      lbm_destroy(c);
+      return LBM_ERR_NOMEM;
+    }
+  }
+  e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    lbm_destroy(c);
+    return LBM_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  c->red_blocks = (int)std::min<int64_t>((c->n + kRedThreads - 1) / kRedThreads, 152 * 4);
+  if (cudaMalloc(&c->d_partial, (size_t)c->red_blocks * kRedMaxK * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->d_out, kRedMaxK * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&c->h_out, kRedMaxK * sizeof(double)) != cudaSuccess) {
+    lbm_destroy(c);
+    return LBM_ERR_NOMEM;
+  }
+  if (d->force_kind == LBM_FORCE_FIELD) {
+    if (cudaMalloc(&c->d_force, (size_t)c->n * 2 * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(c->d_force, d->force_field, (size_t)c->n * 2 * sizeof(double), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+      lbm_destroy(c);
+      return LBM_ERR_NOMEM;
+    }
+  }
+  if (d->force_kind == LBM_FORCE_SHEAR) {
+    if (cudaMalloc(&c->d_xr, (size_t)c->nx * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->d_yr, (size_t)c->ny * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(c->d_xr, d->x_coords, (size_t)c->nx * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->d_yr, d->y_coords, (size_t)c->ny * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+      lbm_destroy(c);
+      return LBM_ERR_NOMEM;
+    }
+  }
+  if (c->coll == LBM_ITERATIVE_INIT) {
+    const size_t cnt = (size_t)c->n * c->Q;
+    if (c->storage == LBM_STORE_F64) {
+      if (cudaMalloc(&c->d_nonlinear, cnt * sizeof(double)) != cudaSuccess ||
+          cudaMemcpy(c->d_nonlinear, d->nonlinear, cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        lbm_destroy(c);
+        return LBM_ERR_NOMEM;
+      }
+    } else {
+      std::vector<float> tmp(cnt);
+      for (size_t k = 0; k < cnt; ++k) tmp[k] = (float)d->nonlinear[k];
+      if (cudaMalloc(&c->d_nonlinear, cnt * sizeof(float)) != cudaSuccess ||
+          cudaMemcpy(c->d_nonlinear, tmp.data(), cnt * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+        lbm_destroy(c);
+        return LBM_ERR_NOMEM;
+      }
+    }
+  }
+  p.Ffield = q.Ffield = c->d_force;
+  p.xr = q.xr = c->d_xr;
+  p.yr = q.yr = c->d_yr;
+  p.nonlinear = static_cast<const double*>(c->d_nonlinear);
+  q.nonlinear = static_cast<const float*>(c->d_nonlinear);
+  *out = c;
+  return LBM_OK;
+}
+
+void lbm_destroy(lbm_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_graphs(c);
+  for (int k = 0; k < 2; ++k) cudaFree(c->buf[k]);
+  cudaFree(c->d_force);
+  cudaFree(c->d_xr);
+  cudaFree(c->d_yr);
+  cudaFree(c->d_nonlinear);
+  cudaFree(c->d_stage);
+  cudaFree(c->d_partial);
+  cudaFree(c->d_out);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  cudaFree(c->d_uold);
+  cudaFree(c->d_analytic);
+  cudaFree(c->d_macro);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+int32_t lbm_set_stream(lbm_ctx* c, void* stream) {
+  if (!c) return LBM_ERR_INVALID;
+  cudaSetDevice(c->device);
+  LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  free_graphs(c);  // graphs are captured on, and launched into, a stream; recapture lazily
+  return LBM_OK;
+}
+
+int32_t lbm_synchronize(lbm_ctx* c) {
+  if (!c) return LBM_ERR_INVALID;
+  cudaSetDevice(c->device);
+  LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return LBM_OK;
+}
+
+static int upload_impl(lbm_ctx* c, const double* f, cudaMemcpyKind kind) {
+  if (!c || !f) return LBM_ERR_INVALID;
+  cudaSetDevice(c->device);
+  const size_t cnt = (size_t)c->n * c->Q;
+  if (c->storage == LBM_STORE_F64) {
+    LBM_CUDA(c, cudaMemcpyAsync(c->buf[0], f, cnt * sizeof(double), kind, c->stream));
+  } else {
+    int rc = ensure(c, &c->d_stage, cnt * sizeof(double));
+    if (rc) return rc;
+    LBM_CUDA(c, cudaMemcpyAsync(c->d_stage, f, cnt * sizeof(double), kind, c->stream));
+    OpArgs a = base_args(c, OP_NARROW);
+    a.src = c->d_stage;
+    a.dst = c->buf[0];
+    rc = run(c, a);
+    if (rc) return rc;
+  }
+  c->cur = 0;
+  c->phase = POST_STREAM;
+  c->have_state = true;
+  LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return LBM_OK;
+}
+
+int32_t lbm_upload(lbm_ctx* c, const double* f) { return upload_impl(c, f, cudaMemcpyHostToDevice); }
+int32_t lbm_upload_device(lbm_ctx* c, const double* f) { return upload_impl(c, f, cudaMemcpyDeviceToDevice); }
+
+static int download_impl(lbm_ctx* c, double* f, cudaMemcpyKind kind) {
+  if (!c || !f) return LBM_ERR_INVALID;
+  if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
+  cudaSetDevice(c->device);
+  const size_t cnt = (size_t)c->n * c->Q;
+  if (c->storage == LBM_STORE_F64) {
+    int rc = materialise(c);
+    if (rc) return rc;
+    LBM_CUDA(c, cudaMemcpyAsync(f, c->buf[c->cur], cnt * sizeof(double), kind, c->stream));
+  } else {
+    int rc = ensure(c, &c->d_stage, cnt * sizeof(double));
+    if (rc) return rc;
+    OpArgs a = base_args(c, OP_WIDEN);
+    a.pull = c->phase == POST_COLLIDE;
+    a.src = c->buf[c->cur];
+    a.dst = c->d_stage;
+    rc = run(c, a);
+    if (rc) return rc;
+    LBM_CUDA(c, cudaMemcpyAsync(f, c->d_stage, cnt * sizeof(double), kind, c->stream));
+  }
+  LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return LBM_OK;
+}
+
+int32_t lbm_download(lbm_ctx* c, double* f) { return download_impl(c, f, cudaMemcpyDeviceToHost); }
+int32_t lbm_download_device(lbm_ctx* c, double* f) { return download_impl(c, f, cudaMemcpyDeviceToDevice); }
+
+int32_t lbm_step(lbm_ctx* c, int64_t nsteps, int64_t t0, double dt) {
+  if (!c || nsteps < 0) return LBM_ERR_INVALID;
+  if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
+  cudaSetDevice(c->device);
+  c->last_launches = 0;
+  int64_t k = 0;
+  const bool time_dependent = c->force_kind == LBM_FORCE_SHEAR;
+  const size_t bytes = (size_t)c->n * c->Q * c->elem;
+  const bool use_graph = !time_dependent && bytes <= kGraphMaxBytes;
+  while (k < nsteps) {
+    set_time(c, (double)(t0 + k) * dt);
+    if (use_graph && c->phase == POST_COLLIDE && nsteps - k >= kGraphSteps) {
+      cudaGraphExec_t g = nullptr;
+      int rc = graph_for_parity(c, c->cur, &g);
+      if (rc) return rc;
+      LBM_CUDA(c, cudaGraphLaunch(g, c->stream));
+      c->last_launches += kGraphSteps;
+      k += kGraphSteps;  // even number of steps: the state returns to the same buffer
+      continue;
+    }
+    int rc = step_once(c);
+    if (rc) return rc;
+    ++k;
+  }
+  return LBM_OK;
+}
+
+int32_t lbm_reduce(lbm_ctx* c, int32_t kind, const lbm_analytic* an, double* out) {
+  if (!c || !out) return LBM_ERR_INVALID;
+  if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
+  cudaSetDevice(c->device);
+  const bool pull = c->phase == POST_COLLIDE;
+  if (kind == LBM_REDUCE_DENSITY_AT) {
+    const int64_t ix = (int64_t)out[0], iy = (int64_t)out[1];
+    if (ix < 0 || ix >= c->nx || iy < 0 || iy >= c->ny) return fail(c, LBM_ERR_INVALID, "node out of range");
+    OpArgs a = base_args(c, OP_NODE_DENSITY);
+    a.pull = pull;
+    a.src = c->buf[c->cur];
+    a.node_x = (int)ix;
+    a.node_y = (int)iy;
+    a.out = c->d_out;
+    int rc = run(c, a);
+    if (rc) return rc;
+    LBM_CUDA(c, cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+    out[0] = c->h_out[0];
+    return LBM_OK;
+  }
+  const int K = red_kind_k(kind);
+  if (!K) return fail(c, LBM_ERR_INVALID, "unknown reduction kind");
+  ReduceArgs r = c->red;
+  r.kind = kind;
+  if (kind == LBM_REDUCE_TRACK_ERRORS || kind == LBM_REDUCE_COMPARE) {
+    if (!an) return fail(c, LBM_ERR_INVALID, "analytic fields required");
+    const double* src[8] = {an->rho, an->ux, an->uy, an->p, an->sxx, an->syx, an->sxy, an->syy};
+    const int need = kind == LBM_REDUCE_TRACK_ERRORS ? 8 : 4;
+    for (int k = 0; k < need; ++k)
+      if (!src[k]) return fail(c, LBM_ERR_INVALID, "missing analytic field");
+    const double* dptr[8];
+    if (an->on_device) {
+      for (int k = 0; k < 8; ++k) dptr[k] = src[k];
+    } else {
+      int rc = ensure(c, &c->d_analytic, (size_t)c->n * 8 * sizeof(double));
+      if (rc) return rc;
+      for (int k = 0; k < 8; ++k) {
+        dptr[k] = c->d_analytic + (size_t)k * c->n;
+        if (src[k])
+          LBM_CUDA(c, cudaMemcpyAsync((void*)dptr[k], src[k], (size_t)c->n * sizeof(double), cudaMemcpyHostToDevice,
+                                      c->stream));
+      }
+    }
+    r.rho_a = dptr[0];
+    r.ux_a = dptr[1];
+    r.uy_a = dptr[2];
+    r.p_a = dptr[3];
+    r.sxx_a = dptr[4];
+    r.syx_a = dptr[5];
+    r.sxy_a = dptr[6];
+    r.syy_a = dptr[7];
+    r.tau = an->tau;
+    r.u_max = an->u_max;
+    r.area = an->area;
+  }
+  if (kind == LBM_REDUCE_VELOCITY_CONVERGENCE) {
+    if (!c->d_uold) {
+      int rc = ensure(c, &c->d_uold, (size_t)c->n * 2 * sizeof(double));
+      if (rc) return rc;
+      LBM_CUDA(c, cudaMemsetAsync(c->d_uold, 0, (size_t)c->n * 2 * sizeof(double), c->stream));
+    }
+    r.u_old = c->d_uold;
+  }
+  OpArgs a = base_args(c, OP_REDUCE);
+  a.red = &r;
+  a.red_k = K;
+  a.pull = pull;
+  a.src = c->buf[c->cur];
+  a.partial = c->d_partial;
+  a.nblocks = c->red_blocks;
+  a.out = c->d_out;
+  int rc = run(c, a);
+  if (rc) return rc;
+  LBM_CUDA(c, cudaMemcpyAsync(c->h_out, c->d_out, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < K; ++k) out[k] = c->h_out[k];
+  if (kind == LBM_REDUCE_CONSERVED && out[3] != 0.0) return fail(c, LBM_ERR_NONFINITE, "non-finite populations");
+  return LBM_OK;
+}
+
+int32_t lbm_macroscopic(lbm_ctx* c, double* rho, double* ux, double* uy) {
+  if (!c) return LBM_ERR_INVALID;
+  if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
+  cudaSetDevice(c->device);
+  int rc = ensure(c, &c->d_macro, (size_t)c->n * 3 * sizeof(double));
+  if (rc) return rc;
+  OpArgs a = base_args(c, OP_MACRO);
+  a.pull = c->phase == POST_COLLIDE;
+  a.src = c->buf[c->cur];
+  a.dst = c->d_macro;
+  rc = run(c, a);
+  if (rc) return rc;
+  double* outs[3] = {rho, ux, uy};
+  for (int k = 0; k < 3; ++k)
+    if (outs[k])
+      LBM_CUDA(c, cudaMemcpyAsync(outs[k], c->d_macro + (size_t)k * c->n, (size_t)c->n * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+  LBM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return LBM_OK;
+}
+
+int32_t lbm_collide_device(lbm_ctx* c, const double* f_in, double* f_out, double time) {
+  if (!c || !f_in || !f_out) return LBM_ERR_INVALID;
+  if (c->storage != LBM_STORE_F64) return fail(c, LBM_ERR_UNSUPPORTED, "device operators need FP64 storage");
+  cudaSetDevice(c->device);
+  set_time(c, time);
+  OpArgs a = base_args(c, OP_COLLIDE);
+  a.src = f_in;
+  a.dst = f_out;
+  return run(c, a);
+}
+
+int32_t lbm_stream_device(lbm_ctx* c, const double* f, double* f_new) {
+  if (!c || !f || !f_new) return LBM_ERR_INVALID;
+  if (c->storage != LBM_STORE_F64) return fail(c, LBM_ERR_UNSUPPORTED, "device operators need FP64 storage");
+  cudaSetDevice(c->device);
+  OpArgs a = base_args(c, OP_STREAM);
+  a.src = f;
+  a.dst = f_new;
+  return run(c, a);
+}
+
+int32_t lbm_apply_bcs_device(lbm_ctx* c, double* f_new, const double* f_old) {
+  if (!c || !f_new || !f_old) return LBM_ERR_INVALID;
+  if (c->storage != LBM_STORE_F64) return fail(c, LBM_ERR_UNSUPPORTED, "device operators need FP64 storage");
+  cudaSetDevice(c->device);
+  if (c->pd.nbc == 0) return LBM_OK;
+  OpArgs a = base_args(c, OP_APPLY_BC);
+  a.src = f_old;
+  a.dst = f_new;
+  return run(c, a);
+}
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+// lbm_common.cuh -- velocity sets, storage traits and kernel parameter blocks shared by the
+// collide-stream kernels (lbm_step.cuh), the reductions (lbm_reduce.cuh) and the C ABI
+// (lbm_api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/lbm_gb300.h"
+
+namespace lbm {
+
+// ---------------------------------------------------------------------------------------
+// Velocity sets.  Abscissae and opposite maps as in src/quadratures/D2Q*.jl and
+// src/quadratures.jl:11-19 (0-based).  The tables are compile-time so that every neighbour
+// offset of the unrolled per-population loops folds to a register or an immediate.
+//   R     : largest |c| component (halo radius of the pull)
+//   EQ    : truncation order of `equilibrium!` (velocity_distribution_function/*.jl)
+//   HN    : Hermite order of the regularised MRT, div(order(q), 2) (mrt.jl:147)
+// ---------------------------------------------------------------------------------------
+#define LBM_DEFINE_LATTICE(NAME, ID, QQ, RR, EQQ, HNN, CXS, CYS, OPS)                    \
+  struct NAME {                                                                           \
+    static constexpr int id = ID, Q = QQ, R = RR, EQ = EQQ, HN = HNN;                     \
+    __host__ __device__ __forceinline__ static constexpr int cx(int i) {                  \
+      constexpr int t[QQ] = CXS;                                                          \
+      return t[i];                                                                        \
+    }                                                                                     \
+    __host__ __device__ __forceinline__ static constexpr int cy(int i) {                  \
+      constexpr int t[QQ] = CYS;                                                          \
+      return t[i];                                                                        \
+    }                                                                                     \
+    __host__ __device__ __forceinline__ static constexpr int opp(int i) {                 \
+      constexpr int t[QQ] = OPS;                                                          \
+      return t[i];                                                                        \
+    }                                                                                     \
+  };
+
+#define LBM_L(...) {__VA_ARGS__}
+LBM_DEFINE_LATTICE(D2Q4, 0, 4, 1, 1, 1, LBM_L(1, 0, -1, 0), LBM_L(0, 1, 0, -1), LBM_L(2, 3, 0, 1))
+LBM_DEFINE_LATTICE(D2Q5, 1, 5, 1, 1, 1, LBM_L(0, 1, 0, -1, 0), LBM_L(0, 0, 1, 0, -1), LBM_L(0, 3, 4, 1, 2))
+LBM_DEFINE_LATTICE(D2Q9, 2, 9, 1, 2, 2, LBM_L(0, -1, -1, -1, 0, 1, 1, 1, 0),
+                   LBM_L(0, 1, 0, -1, -1, -1, 0, 1, 1), LBM_L(0, 5, 6, 7, 8, 1, 2, 3, 4))
+LBM_DEFINE_LATTICE(D2Q13, 3, 13, 2, 2, 2, LBM_L(0, 1, -1, 0, 0, 1, -1, 1, -1, 2, -2, 0, 0),
+                   LBM_L(0, 0, 0, 1, -1, 1, -1, -1, 1, 0, 0, -2, 2),
+                   LBM_L(0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11))
+LBM_DEFINE_LATTICE(D2Q17, 4, 17, 3, 3, 3, LBM_L(0, 1, -1, 0, 0, 1, -1, 1, -1, 2, -2, 2, -2, 3, -3, 0, 0),
+                   LBM_L(0, 0, 0, 1, -1, 1, -1, -1, 1, 2, -2, -2, 2, 0, 0, 3, -3),
+                   LBM_L(0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15))
+LBM_DEFINE_LATTICE(D2Q21, 5, 25, 3, 3, 3,
+                   LBM_L(0, 1, -1, 0, 0, 1, -1, 1, -1, 2, -2, 0, 0, 2, -2, 2, -2, 3, -3, 0, 0, 3, -3, -3, 3),
+                   LBM_L(0, 0, 0, 1, -1, 1, -1, -1, 1, 0, 0, 2, -2, 2, -2, -2, 2, 0, 0, 3, -3, 3, -3, 3, -3),
+                   LBM_L(0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17, 20, 19, 22, 21,
+                         24, 23))
+LBM_DEFINE_LATTICE(D2Q37, 6, 37, 3, 4, 4,
+                   LBM_L(0, 1, -1, 0, 0, 1, -1, 1, -1, 2, -2, 0, 0, 2, -2, -2, 2, 1, -1, 1, -1, 2, -2, 2, -2,
+                         3, -3, 0, 0, 3, -3, 3, -3, 1, -1, -1, 1),
+                   LBM_L(0, 0, 0, 1, -1, 1, -1, -1, 1, 0, 0, 2, -2, 1, -1, 1, -1, 2, -2, -2, 2, 2, -2, -2, 2,
+                         0, 0, 3, -3, 1, -1, -1, 1, 3, -3, 3, -3),
+                   LBM_L(0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17, 20, 19, 22, 21,
+                         24, 23, 26, 25, 28, 27, 30, 29, 32, 31, 34, 33, 36, 35))
+#undef LBM_L
+
+// ---------------------------------------------------------------------------------------
+// Storage traits.  F64 stores f; F32Dev / F16Dev store g = f - w and compute in FP32.
+// ---------------------------------------------------------------------------------------
+struct F64 {
+  using T = double;     // element in HBM
+  using C = double;     // compute type
+  static constexpr bool DEV = false;
+  static constexpr int id = LBM_STORE_F64;
+  __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
+  __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
+};
+struct F32Dev {
+  using T = float;
+  using C = float;
+  static constexpr bool DEV = true;
+  static constexpr int id = LBM_STORE_F32_DEV;
+  __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
+  __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
+};
+struct F16Dev {
+  using T = __half;
+  using C = float;
+  static constexpr bool DEV = true;
+  static constexpr int id = LBM_STORE_F16_DEV;
+  __device__ __forceinline__ static C ld(const T* p) { return __half2float(__ldg(p)); }
+  __device__ __forceinline__ static void st(T* p, C v) { *p = __float2half_rn(v); }
+};
+
+// ---------------------------------------------------------------------------------------
+// Kernel parameter blocks (passed by value; they live in the constant bank).
+// ---------------------------------------------------------------------------------------
+struct BCDev {
+  int kind, dir;
+  int x_lo, x_hi, y_lo, y_hi;  // 0-based inclusive
+  double add[LBM_MAX_Q];       // MOVING_WALL: 2 * a_1 per population (moving_wall.jl:20-33)
+};
+
+template <class CT>
+struct StepParams {
+  int nx, ny;
+  long long n;                 // plane stride nx * ny
+  int dxm[7], dym[7];          // (d mod nx), (d mod ny) for d = -3..3 (periodic pull offsets)
+  CT w[LBM_MAX_Q];
+  CT cs;                       // 1 / c_s^2 (the reference's speed_of_sound_squared)
+  CT om_a, om_b;               // SRT: (1 - 1/τ), 1/τ ; ITER: same
+  CT inv_ts, inv_ta;           // TRT: 1/τ_s, 1/τ_a
+  CT shift;                    // force velocity shift: τ (SRT), τ_a (TRT), τs[2] (MRT)
+  CT mrt_a[4], mrt_b[4];       // MRT: (1 - 1/τ_n), 1/τ_n for n = 1..4
+  int force_kind;
+  CT F[2];                     // CONSTANT force
+  const double* Ffield;        // FIELD force planes (device)
+  double shear[6];             // SHEAR force
+  const double* xr;            // SHEAR coordinates (device)
+  const double* yr;
+  double time;                 // physical time of this step
+  const CT* nonlinear;         // ITER: nonlinear equilibrium term planes (device)
+  int nbc;
+  BCDev bc[LBM_MAX_BC];
+};
+
+}  // namespace lbm

@@ -1,0 +1,7 @@
+// Kernel instantiations for the D2Q37 velocity set (separate translation unit so the
+// velocity sets compile in parallel).
+#include "lbm_ops.cuh"
+
+namespace lbm {
+cudaError_t run_op_q37(const OpArgs& a) { return run_op<D2Q37>(a); }
+}  // namespace lbm

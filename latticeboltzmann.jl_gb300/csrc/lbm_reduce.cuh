@@ -1,0 +1,295 @@
+// lbm_reduce.cuh -- whole-lattice reductions for the processing methods (next!).
+//
+// Each kernel reads the populations of the state the reference's next!(pm, q, f_stream, t)
+// observes: when the device holds the post-collision array, the periodic pull and the
+// boundary conditions are applied on the fly (load_streamed), so no extra pass over the
+// lattice is made.  Moments are formed in FP64 whatever the storage (deviation storage is
+// widened as f = w + g), and the per-block partial sums are combined by a single block in
+// a fixed order, so results are bitwise reproducible run to run.
+#pragma once
+
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedMaxK = 16;
+
+struct ReduceArgs {
+  int kind;
+  double w[LBM_MAX_Q];
+  double cs;                        // 1 / c_s^2
+  const double *rho_a, *ux_a, *uy_a, *p_a, *sxx_a, *syx_a, *sxy_a, *syy_a;  // analytic fields (device)
+  double tau;                       // (1/c_s²)·ν for the stress estimate
+  double u_max;
+  double area;
+  double* u_old;                    // VELOCITY_CONVERGENCE: 2 planes (device)
+  int q_low_order;                  // D2Q4 / D2Q5: pressure(q, f, ρ, u) is the constant 1
+};
+
+template <int K>
+__device__ __forceinline__ void block_reduce_store(double (&acc)[K], double* partial) {
+  __shared__ double sh[kRedThreads / 32][K];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int wi = 0; wi < kRedThreads / 32; ++wi) s += sh[wi][threadIdx.x];
+    partial[(size_t)blockIdx.x * K + threadIdx.x] = s;
+  }
+}
+
+// Per-node moments in FP64 of the observed populations.
+template <class L, class S, bool PULL>
+__device__ __forceinline__ void node_f64(const StepParams<typename S::C>& p, const ReduceArgs& r,
+                                         const typename S::T* __restrict__ src, int x, int y, double* f) {
+  using CT = typename S::C;
+  CT v[L::Q];
+  if (PULL) load_streamed<L, S>(p, src, x, y, v);
+  else load_local<L, S>(p, src, y * p.nx + x, v);
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) f[i] = S::DEV ? r.w[i] + (double)v[i] : (double)v[i];
+}
+
+template <class L, class S, bool PULL, int K>
+__global__ void __launch_bounds__(kRedThreads) reduce_kernel(StepParams<typename S::C> p, ReduceArgs r,
+                                                             const typename S::T* __restrict__ src,
+                                                             double* __restrict__ partial) {
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  const long long total = p.n;
+  const double ics = 1.0 / r.cs;
+  for (long long node = (long long)blockIdx.x * kRedThreads + threadIdx.x; node < total;
+       node += (long long)gridDim.x * kRedThreads) {
+    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+    double f[L::Q];
+    node_f64<L, S, PULL>(p, r, src, x, y, f);
+    double rho = f[0];
+#pragma unroll
+    for (int i = 1; i < L::Q; ++i) rho += f[i];
+    double jx = 0.0, jy = 0.0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      jx += f[i] * L::cx(i);
+      jy += f[i] * L::cy(i);
+    }
+    const double ux = jx / rho, uy = jy / rho;
+    if (K == 16) {  // TRACK_ERRORS, track_hydrodynamic_errors.jl:114-203
+      double axx = 0.0, axy = 0.0, ayy = 0.0;  // a_bar_2 = Σ f H_2(c)
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        axx += f[i] * ((double)(L::cx(i) * L::cx(i)) - ics);
+        axy += f[i] * (double)(L::cx(i) * L::cy(i));
+        ayy += f[i] * ((double)(L::cy(i) * L::cy(i)) - ics);
+      }
+      const double exx = rho * (ux * ux), exy = rho * (ux * uy), eyy = rho * (uy * uy);  // a_eq_2, T = 1
+      const double tau = r.tau;
+      const double h = 1.0 / (2.0 * tau), den = 1.0 + 1.0 / (2.0 * tau);
+      const double A2xx = (axx + h * exx) / den, A2yy = (ayy + h * eyy) / den;
+      const double Pxx = A2xx - rho * (ux * ux - 1.0), Pyy = A2yy - rho * (uy * uy - 1.0);
+      const double pr = (Pxx + Pyy) / 2.0;
+      // deviatoric_tensor(q, τ, f, ρ, u), moments.jl:81-96
+      const double sxx0 = (axx - exx) / den, sxy0 = (axy - exy) / den, syy0 = (ayy - eyy) / den;
+      const double tr = (sxx0 + syy0) / 2.0;
+      const double fac = 1.0 / (r.u_max * r.u_max);
+      const double sxx = (sxx0 - tr) * fac, sxy = sxy0 * fac, syy = (syy0 - tr) * fac, syx = sxy;
+      const double udx = ux / r.u_max, udy = uy / r.u_max;
+      const size_t k = (size_t)node;
+      const double erho = r.rho_a[k], eux = r.ux_a[k], euy = r.uy_a[k], ep = r.p_a[k];
+      const double esxx = r.sxx_a[k], esyx = r.syx_a[k], esxy = r.sxy_a[k], esyy = r.syy_a[k];
+      acc[0] += (rho - erho) * (rho - erho);
+      acc[1] += (udx - eux) * (udx - eux) + (udy - euy) * (udy - euy);
+      acc[2] += (pr - ep) * (pr - ep);
+      acc[3] += (esxx - sxx) * (esxx - sxx);
+      acc[4] += (esxy - sxy) * (esxy - sxy);
+      acc[5] += (esyy - syy) * (esyy - syy);
+      acc[6] += (esyx - syx) * (esyx - syx);
+      acc[7] += eux * eux + euy * euy;
+      acc[8] += esxx * esxx;
+      acc[9] += esyy * esyy;
+      acc[10] += esxy * esxy;
+      acc[11] += esyx * esyx;
+      acc[12] += ep * ep;
+      acc[13] += rho;
+      acc[14] += rho * (udx + udy);
+      acc[15] += rho * (udx * udx + udy * udy);
+    } else if (K == 12) {  // COMPARE, processing_methods.jl:177-239
+      double pr;
+      if (r.q_low_order) {
+        pr = 1.0;
+      } else {
+        double axx = 0.0, ayy = 0.0;
+#pragma unroll
+        for (int i = 0; i < L::Q; ++i) {
+          axx += f[i] * ((double)(L::cx(i) * L::cx(i)) - ics);
+          ayy += f[i] * ((double)(L::cy(i) * L::cy(i)) - ics);
+        }
+        pr = ((axx + ayy) - rho * ((ux * ux + uy * uy) - 2.0)) / 2.0;  // moments.jl:21-33
+      }
+      const double T = pr / rho;
+      const double udx = ux / r.u_max, udy = uy / r.u_max;
+      const double ke = (udx * udx + udy * udy) * rho;
+      const size_t k = (size_t)node;
+      const double erho = r.rho_a[k], ep = r.p_a[k], eux = r.ux_a[k], euy = r.uy_a[k];
+      const double eT = ep / erho, eke = eux * eux + euy * euy;
+      acc[0] += rho;
+      acc[1] += (udx + udy) * rho;
+      acc[2] += ke + T;
+      acc[3] += ke;
+      acc[4] += T;
+      acc[5] += erho;
+      acc[6] += erho * (eux + euy);
+      acc[7] += eke + eT;
+      acc[8] += eke;
+      acc[9] += eT;
+      acc[10] += r.area * ((udx - eux) * (udx - eux) + (udy - euy) * (udy - euy));
+      acc[11] += r.area * ((pr - ep) * (pr - ep));
+    } else if (K == 2) {  // MEAN_VELOCITY (stopping_criteria.jl:43-54)
+      acc[0] += ux;
+      acc[1] += 1.0;
+    } else if (K == 3) {  // VELOCITY_CONVERGENCE (stopping_criteria.jl:101-116)
+      const size_t k = (size_t)node;
+      const double ox = r.u_old[k], oy = r.u_old[p.n + k];
+      acc[0] += (ux - ox) * (ux - ox) + (uy - oy) * (uy - oy);
+      acc[1] += ox * ox + oy * oy;
+      r.u_old[k] = ux;
+      r.u_old[p.n + k] = uy;
+    } else if (K == 4) {  // CONSERVED
+      acc[0] += rho;
+      acc[1] += jx;
+      acc[2] += jy;
+      int bad = 0;
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) bad += isfinite(f[i]) ? 0 : 1;
+      acc[3] += bad;
+    }
+  }
+  block_reduce_store<K>(acc, partial);
+}
+
+// Sums the per-block partials in block order (deterministic).
+template <int K>
+__global__ void reduce_finish_kernel(const double* __restrict__ partial, int nblocks, double* __restrict__ out) {
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * K + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+// ρ, ux, uy planes of the observed state (density / velocity!, moments.jl:1-19).
+template <class L, class S, bool PULL>
+__global__ void __launch_bounds__(kBlockX) macro_kernel(StepParams<typename S::C> p, ReduceArgs r,
+                                                        const typename S::T* __restrict__ src,
+                                                        double* __restrict__ out) {
+  const int x = blockIdx.x * kBlockX + threadIdx.x;
+  if (x >= p.nx) return;
+  for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
+    double f[L::Q];
+    node_f64<L, S, PULL>(p, r, src, x, y, f);
+    double rho = f[0];
+#pragma unroll
+    for (int i = 1; i < L::Q; ++i) rho += f[i];
+    double jx = 0.0, jy = 0.0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      jx += f[i] * L::cx(i);
+      jy += f[i] * L::cy(i);
+    }
+    const size_t k = (size_t)y * p.nx + x;
+    out[k] = rho;
+    out[p.n + k] = jx / rho;
+    out[2 * p.n + k] = jy / rho;
+  }
+}
+
+// Observed populations as FP64 planes (download of deviation storage, or materialisation).
+template <class L, class S, bool PULL>
+__global__ void __launch_bounds__(kBlockX) widen_kernel(StepParams<typename S::C> p, ReduceArgs r,
+                                                        const typename S::T* __restrict__ src,
+                                                        double* __restrict__ out) {
+  const int x = blockIdx.x * kBlockX + threadIdx.x;
+  if (x >= p.nx) return;
+  for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
+    double f[L::Q];
+    node_f64<L, S, PULL>(p, r, src, x, y, f);
+    const size_t k = (size_t)y * p.nx + x;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) out[(size_t)i * p.n + k] = f[i];
+  }
+}
+
+// FP64 planes -> storage (upload): f for F64, g = f - w (rounded once) for deviation storage.
+template <class L, class S>
+__global__ void __launch_bounds__(kBlockX) narrow_kernel(StepParams<typename S::C> p, ReduceArgs r,
+                                                         const double* __restrict__ in,
+                                                         typename S::T* __restrict__ dst) {
+  const int x = blockIdx.x * kBlockX + threadIdx.x;
+  if (x >= p.nx) return;
+  for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
+    const size_t k = (size_t)y * p.nx + x;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const double f = in[(size_t)i * p.n + k];
+      S::st(dst + (size_t)i * p.n + k, (typename S::C)(S::DEV ? f - r.w[i] : f));
+    }
+  }
+}
+
+// Density of one node of the observed state (DensityConvergence, density_convergence.jl:6-17).
+template <class L, class S, bool PULL>
+__global__ void node_density_kernel(StepParams<typename S::C> p, ReduceArgs r, const typename S::T* __restrict__ src,
+                                    int x, int y, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double f[L::Q];
+  node_f64<L, S, PULL>(p, r, src, x, y, f);
+  double rho = f[0];
+#pragma unroll
+  for (int i = 1; i < L::Q; ++i) rho += f[i];
+  out[0] = rho;
+}
+
+// apply!(bcs, q, f_new, f_old) on FP64 arrays in place (the single-operator entry point).
+template <class L>
+__global__ void __launch_bounds__(kBlockX) apply_bcs_kernel(StepParams<double> p, double* __restrict__ fnew,
+                                                            const double* __restrict__ fold) {
+  const int x = blockIdx.x * kBlockX + threadIdx.x;
+  if (x >= p.nx) return;
+  for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
+  if (!(y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R)) continue;
+  const int node = y * p.nx + x;
+  const int y1 = y + 1, x1 = x + 1;
+  for (int b = 0; b < p.nbc; ++b) {
+    const BCDev& bc = p.bc[b];
+    if (bc.kind == LBM_BOUNCE_BACK) {
+      if (x < bc.x_lo || x > bc.x_hi || y < bc.y_lo || y > bc.y_hi) continue;
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const int o = L::opp(i);
+        bool hit;
+        if (bc.dir == LBM_NORTH) hit = y1 + L::cy(o) > p.ny;
+        else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
+        else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
+        else hit = x1 + L::cx(o) <= 0;
+        if (hit) fnew[(size_t)i * p.n + node] = fold[(size_t)o * p.n + node];
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const int o = L::opp(i);
+        if (y1 + L::cy(o) > p.ny) fnew[(size_t)i * p.n + node] = fold[(size_t)o * p.n + node] + bc.add[i];
+      }
+    }
+  }
+  }
+}
+
+}  // namespace lbm

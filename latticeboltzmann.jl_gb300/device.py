@@ -1,0 +1,204 @@
+"""DeviceLattice: one liblbm_gb300 context (the populations of one lattice on the GPU plus
+its quadrature, collision model and boundary list), wrapped for Python callers.
+
+Populations cross the boundary in the reference's Julia layout f[x, y, i]; in numpy that is
+a C-contiguous float64 array of shape (Q, NY, NX).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .boundary_conditions import BounceBack, MovingWall
+from .collision_models import MRT, SRT, TRT, IterativeInitializationCollisionModel
+
+
+def _as_f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+class DeviceLattice:
+    """A lattice of nx x ny nodes with populations resident in HBM.
+
+    force: None | ("constant", (Fx, Fy)) | ("field", array (2, NY, NX)) |
+           ("shear", [c0..c5], x_coords, y_coords)
+    storage: "f64" | "f32dev" | "f16dev"
+    nonlinear: the (Q, NY, NX) term of the iterative-initialisation collision model
+    """
+
+    def __init__(self, q, nx, ny, collision_model, bcs=(), force=None, storage="f64", nonlinear=None):
+        L = N.lib()
+        self.q = q
+        self.nx, self.ny = int(nx), int(ny)
+        self.Q = q.Q
+        self.shape = (self.Q, self.ny, self.nx)
+        self.storage = storage
+        d = N.LbmDesc()
+        d.quadrature = q.qid
+        for i, w in enumerate(q.weights):
+            d.weights[i] = float(w)
+        d.speed_of_sound_squared = q.speed_of_sound_squared
+        cm = collision_model
+        if isinstance(cm, SRT):
+            d.collision, taus = N.SRT, [cm.τ]
+        elif isinstance(cm, TRT):
+            d.collision, taus = N.TRT, [cm.τ_symmetric, cm.τ_asymmetric]
+        elif isinstance(cm, MRT):
+            d.collision = N.MRT
+            taus = list(cm.τs) + [1.0] * max(0, 4 - len(cm.τs))
+        elif isinstance(cm, IterativeInitializationCollisionModel):
+            d.collision, taus = N.ITERATIVE_INIT, [cm.τ]
+        else:
+            raise TypeError(f"unsupported collision model {cm!r}")
+        for k, t in enumerate(taus[:4]):
+            d.tau[k] = float(t)
+        self._keep = []
+        d.force_kind = N.FORCE_NONE
+        if force is not None:
+            kind = force[0]
+            if kind == "constant":
+                d.force_kind = N.FORCE_CONSTANT
+                d.force[0], d.force[1] = float(force[1][0]), float(force[1][1])
+            elif kind == "field":
+                ff = _as_f64(force[1], (2, self.ny, self.nx))
+                self._keep.append(ff)
+                d.force_kind = N.FORCE_FIELD
+                d.force_field = ff.ctypes.data_as(N._DP)
+            elif kind == "shear":
+                xr = _as_f64(force[2], (self.nx,))
+                yr = _as_f64(force[3], (self.ny,))
+                self._keep += [xr, yr]
+                d.force_kind = N.FORCE_SHEAR
+                for k in range(6):
+                    d.shear[k] = float(force[1][k])
+                d.x_coords = xr.ctypes.data_as(N._DP)
+                d.y_coords = yr.ctypes.data_as(N._DP)
+            else:
+                raise ValueError(f"unknown force kind {kind}")
+        if nonlinear is not None:
+            nl = _as_f64(nonlinear, self.shape)
+            self._keep.append(nl)
+            d.nonlinear = nl.ctypes.data_as(N._DP)
+        bcs = list(bcs)
+        if len(bcs) > N.MAX_BC:
+            raise ValueError(f"at most {N.MAX_BC} boundary conditions")
+        arr = (N.LbmBC * max(1, len(bcs)))()
+        for k, b in enumerate(bcs):
+            e = arr[k]
+            e.kind = N.BOUNCE_BACK if isinstance(b, BounceBack) else N.MOVING_WALL
+            e.direction = b.direction.code
+            e.x_lo, e.x_hi = b.xs
+            e.y_lo, e.y_hi = b.ys
+            if isinstance(b, MovingWall):
+                e.u[0], e.u[1] = b.u
+                e.rho, e.T = b.ρ, b.T
+        self._keep.append(arr)
+        d.nbc = len(bcs)
+        d.bcs = C.cast(arr, C.POINTER(N.LbmBC))
+        d.nx, d.ny = self.nx, self.ny
+        d.storage = N.STORAGE_IDS[storage]
+        h = C.c_void_p()
+        st = L.lbm_create(C.byref(h), C.byref(d))
+        if st != N.LBM_OK:
+            raise N.LbmError(st, f"lbm_create: {L.lbm_status_string(st).decode()}")
+        self.h = h
+        self._keep = []  # the library copied what it needs
+
+    # ---- lifetime ----------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().lbm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        N.check(self.h, N.lib().lbm_set_stream(self.h, stream_handle or None))
+
+    def synchronize(self):
+        N.check(self.h, N.lib().lbm_synchronize(self.h))
+
+    # ---- populations -------------------------------------------------------------------
+    def upload(self, f):
+        if hasattr(f, "data_ptr"):  # torch tensor
+            if f.is_cuda:
+                N.check(self.h, N.lib().lbm_upload_device(self.h, f.data_ptr()))
+                return
+            N.check(self.h, N.lib().lbm_upload(self.h, f.data_ptr()))
+            return
+        f = _as_f64(f, self.shape)
+        N.check(self.h, N.lib().lbm_upload(self.h, f.ctypes.data))
+
+    def download(self, out=None):
+        if out is not None and hasattr(out, "data_ptr"):
+            fn = N.lib().lbm_download_device if out.is_cuda else N.lib().lbm_download
+            N.check(self.h, fn(self.h, out.data_ptr()))
+            return out
+        out = np.empty(self.shape) if out is None else out
+        N.check(self.h, N.lib().lbm_download(self.h, out.ctypes.data))
+        return out
+
+    def step(self, nsteps: int, t0: int = 0, dt: float = 0.0):
+        N.check(self.h, N.lib().lbm_step(self.h, int(nsteps), int(t0), float(dt)))
+
+    def last_launch_count(self) -> int:
+        return int(N.lib().lbm_last_launch_count(self.h))
+
+    # ---- reductions --------------------------------------------------------------------
+    def reduce(self, kind, fields=None, tau=0.0, u_max=1.0, area=0.0):
+        out = np.zeros(16)
+        an = None
+        keep = []
+        if fields is not None:
+            an = N.LbmAnalytic()
+            for name in ("rho", "ux", "uy", "p", "sxx", "syx", "sxy", "syy"):
+                a = fields.get(name)
+                if a is not None:
+                    if hasattr(a, "data_ptr"):
+                        an.on_device = 1
+                        setattr(an, name, C.cast(C.c_void_p(a.data_ptr()), N._DP))
+                    else:
+                        a = _as_f64(a, (self.ny, self.nx))
+                        keep.append(a)
+                        setattr(an, name, a.ctypes.data_as(N._DP))
+            an.tau, an.u_max, an.area = float(tau), float(u_max), float(area)
+        st = N.lib().lbm_reduce(self.h, int(kind), C.byref(an) if an is not None else None,
+                                out.ctypes.data_as(N._DP))
+        N.check(self.h, st)
+        return out[: N.REDUCE_K[kind]]
+
+    def density_at(self, x: int, y: int) -> float:
+        out = np.zeros(16)
+        out[0], out[1] = x, y
+        N.check(self.h, N.lib().lbm_reduce(self.h, N.REDUCE_DENSITY_AT, None, out.ctypes.data_as(N._DP)))
+        return float(out[0])
+
+    def conserved(self):
+        """Σρ, Σρux, Σρuy over the lattice; raises on non-finite populations."""
+        return self.reduce(N.REDUCE_CONSERVED)[:3]
+
+    def macroscopic(self):
+        rho = np.empty((self.ny, self.nx))
+        ux = np.empty((self.ny, self.nx))
+        uy = np.empty((self.ny, self.nx))
+        N.check(self.h, N.lib().lbm_macroscopic(self.h, rho.ctypes.data, ux.ctypes.data, uy.ctypes.data))
+        return rho, ux, uy
+
+    # ---- single operators on caller-owned device arrays --------------------------------
+    def collide_device(self, f_in, f_out, time=0.0):
+        N.check(self.h, N.lib().lbm_collide_device(self.h, N.ptr(f_in), N.ptr(f_out), float(time)))
+
+    def stream_device(self, f, f_new):
+        N.check(self.h, N.lib().lbm_stream_device(self.h, N.ptr(f), N.ptr(f_new)))
+
+    def apply_bcs_device(self, f_new, f_old):
+        N.check(self.h, N.lib().lbm_apply_bcs_device(self.h, N.ptr(f_new), N.ptr(f_old)))

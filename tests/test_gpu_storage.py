@@ -1,0 +1,67 @@
+"""FP32 / FP16 deviation storage (g = f - w, FP32 arithmetic) against the FP64 path."""
+import numpy as np
+import pytest
+
+from gpu_cases import QUADS, wave_field
+
+pytestmark = pytest.mark.gpu
+
+
+def _velocity(lbm, m):
+    rho, ux, uy = m.lattice.macroscopic()
+    return rho, ux, uy
+
+
+@pytest.mark.parametrize("qname", QUADS)
+@pytest.mark.parametrize("coll", ["SRT", "TRT", "MRT"])
+def test_f32dev_matches_f64(lbm_gpu, qname, coll):
+    lbm = lbm_gpu
+    q = lbm.Quadratures[qname]
+    f0 = wave_field(q, 48, 40, seed=11, amp=0.01)
+    cm = {"SRT": lbm.SRT(0.8), "TRT": lbm.TRT.fields(0.8, 1.0), "MRT": lbm.MRT(q, 0.8)}[coll]
+    out = {}
+    for storage in ("f64", "f32dev"):
+        m = lbm.LatticeBoltzmannModel.from_parts(q, f0, cm, storage=storage)
+        m.lattice.step(200, 0, 0.0)
+        out[storage] = _velocity(lbm, m)
+        m.close()
+    u64 = np.hypot(out["f64"][1], out["f64"][2])
+    du = np.hypot(out["f32dev"][1] - out["f64"][1], out["f32dev"][2] - out["f64"][2])
+    rel_u = float(du.max() / u64.max())
+    drho = float(np.max(np.abs(out["f32dev"][0] - out["f64"][0])))
+    assert rel_u < 1e-5, rel_u
+    assert drho < 1e-6, drho
+
+
+def test_f16dev_runs_and_conserves(lbm_gpu):
+    lbm = lbm_gpu
+    q = lbm.D2Q9()
+    f0 = wave_field(q, 64, 64, seed=2, amp=0.01)
+    res = {}
+    for storage in ("f64", "f16dev"):
+        m = lbm.LatticeBoltzmannModel.from_parts(q, f0, lbm.TRT.fields(0.8, 1.0), storage=storage)
+        m.lattice.step(100, 0, 0.0)
+        res[storage] = _velocity(lbm, m)
+        m.close()
+    u64 = np.hypot(res["f64"][1], res["f64"][2])
+    du = np.hypot(res["f16dev"][1] - res["f64"][1], res["f16dev"][2] - res["f64"][2])
+    assert float(du.max() / u64.max()) < 5e-2
+
+
+@pytest.mark.parametrize("storage", ["f32dev", "f16dev"])
+def test_deviation_storage_with_walls_and_force(lbm_gpu, O, storage):
+    lbm = lbm_gpu
+    q = lbm.D2Q9()
+    nu = (0.9 - 0.5) / 3
+    problem = lbm.PoiseuilleFlow.fields(1.0, 0.1, nu, 3, 32, 1.0, (1.0, 1.0), 1.0)
+    cm = lbm.TRT.fields(0.9, 0.5 + 0.25 / 0.4, "problem")
+    res = {}
+    for st in ("f64", storage):
+        m = lbm.LatticeBoltzmannModel(problem, q, collision_model=cm, storage=st,
+                                      initialization_strategy=lbm.ZeroVelocityInitialCondition())
+        lbm.run_steps(m, 0, 499)
+        res[st] = m.lattice.macroscopic()
+        m.close()
+    ux64 = res["f64"][1]
+    rel = float(np.max(np.abs(res[storage][1] - ux64)) / np.max(np.abs(ux64)))
+    assert rel < (1e-5 if storage == "f32dev" else 5e-2), rel
