@@ -32,7 +32,7 @@ NX = NY = 4096
 Q = 9
 SEED = 20240611
 METRIC = "D2Q9 TRT 4096² MLUPS & %HBM peak: FP64 vs FP32-dev, batched, adjoint"
-BYTES_PER_LU = {"f64": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2}
+BYTES_PER_LU = {"f64": 2 * Q * 8, "df64dev": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2}
 
 
 def tau_from_seed():
@@ -221,7 +221,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--storage", default="f64", choices=["f64", "f32dev", "f16dev"])
+    ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev"])
+    ap.add_argument("--profile", action="store_true",
+                    help="time only the device loop of the chosen storage (for profiler runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -260,21 +262,23 @@ def main():
     achieved_gbs = bytes_lu * NX * NY / per_launch / 1e9
     traffic = profiled_traffic().get(f"step_{args.storage}")
 
-    e2e_s, h2d, d2h = time_e2e(torch, lbm, problem, model, f0, args.steps, dt)
-    e2e = {"value": NX * NY * args.steps / e2e_s / 1e6 * world, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h}
+    e2e = None
+    if not args.profile:
+        e2e_s, h2d, d2h = time_e2e(torch, lbm, problem, model, f0, args.steps, dt)
+        e2e = {"value": NX * NY * args.steps / e2e_s / 1e6 * world, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
     model.close()
 
     extra = {}
-    if args.storage == "f64" and rank == 0:
-        _, m32, _ = build_model(lbm, "f32dev", tau_s)
-        s32, _ = time_device(torch, m32, args.steps, args.warmup, dt)
-        m32.close()
-        extra["f32dev"] = {"value": NX * NY * args.steps / s32 / 1e6, "unit": "MLUPS",
-                           "speedup_vs_f64": seconds / s32,
-                           "roofline_frac": BYTES_PER_LU["f32dev"] * NX * NY / (s32 / args.steps) / 1e9 / peak_gbs}
+    if args.storage == "f64" and rank == 0 and not args.profile:
+        for st in ("df64dev", "f32dev"):
+            _, mx, _ = build_model(lbm, st, tau_s)
+            sx, _ = time_device(torch, mx, args.steps, args.warmup, dt)
+            mx.close()
+            extra[st] = {"value": NX * NY * args.steps / sx / 1e6, "unit": "MLUPS", "speedup_vs_f64": seconds / sx,
+                         "roofline_frac": BYTES_PER_LU[st] * NX * NY / (sx / args.steps) / 1e9 / peak_gbs}
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(tau_s)
     if rank == 0:
         line = {"metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,

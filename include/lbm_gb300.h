@@ -59,9 +59,14 @@ typedef enum { LBM_D2Q4 = 0, LBM_D2Q5, LBM_D2Q9, LBM_D2Q13, LBM_D2Q17, LBM_D2Q21
  *                      ITERATIVE_INIT  src/collision_models/iterative_initialization.jl:1-60 */
 typedef enum { LBM_SRT = 0, LBM_TRT = 1, LBM_MRT = 2, LBM_ITERATIVE_INIT = 3 } lbm_collision_kind;
 
-/* Device storage of the distributions.  F64 keeps f itself; F32_DEV / F16_DEV keep the
- * deviation g_i = f_i - w_i and compute in FP32. */
-typedef enum { LBM_STORE_F64 = 0, LBM_STORE_F32_DEV = 1, LBM_STORE_F16_DEV = 2 } lbm_storage;
+/* Device storage of the distributions.
+ *   F64       f itself, FP64 arithmetic (GB300 runs FP64 at 1/64 of the FP32 rate)
+ *   F32_DEV   the deviation g_i = f_i - w_i in FP32, FP32 arithmetic
+ *   F16_DEV   g_i in FP16, FP32 arithmetic
+ *   DF64_DEV  g_i as a float-float pair (8 bytes, a 48-bit significand on a value far
+ *             smaller than f), float-float arithmetic on the FP32 pipes: FP64-class results
+ *             at the FP64 storage traffic. */
+typedef enum { LBM_STORE_F64 = 0, LBM_STORE_F32_DEV = 1, LBM_STORE_F16_DEV = 2, LBM_STORE_DF64_DEV = 3 } lbm_storage;
 
 /* Forcing, applied as the reference does: a velocity shift of the equilibrium, u + τ F
  * (srt.jl:52-54, trt.jl:76-79, mrt.jl:91-95).

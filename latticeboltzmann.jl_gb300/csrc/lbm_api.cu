@@ -6,7 +6,9 @@
 // the work is issued on.  The device state is either the reference's `f_stream` (after an
 // upload) or the post-collision array of the last step, from which `f_stream` is pulled on
 // demand; see lbm_step.cuh.
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -71,6 +73,7 @@ struct lbm_ctx {
   cudaStream_t own_stream = nullptr, stream = nullptr;
   StepParams<double> pd{};
   StepParams<float> pf{};
+  StepParams<dd> px{};
   ReduceArgs red{};
   double* d_force = nullptr;
   double* d_xr = nullptr;
@@ -114,6 +117,7 @@ OpArgs base_args(lbm_ctx* c, int op) {
   a.coll = c->coll;
   a.pd = &c->pd;
   a.pf = &c->pf;
+  a.px = &c->px;
   a.red = &c->red;
   a.stream = c->stream;
   return a;
@@ -129,6 +133,7 @@ int run(lbm_ctx* c, const OpArgs& a) {
 void set_time(lbm_ctx* c, double t) {
   c->pd.time = t;
   c->pf.time = t;
+  c->px.time = t;
 }
 
 int ensure(lbm_ctx* c, double** p, size_t bytes) {
@@ -245,7 +250,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   *out = nullptr;
   if (d->quadrature < 0 || d->quadrature > 6) return LBM_ERR_INVALID;
   if (d->nx < 1 || d->ny < 1 || d->nx * d->ny >= (int64_t(1) << 31)) return LBM_ERR_INVALID;
-  if (d->storage < 0 || d->storage > 2) return LBM_ERR_INVALID;
+  if (d->storage < 0 || d->storage > 3) return LBM_ERR_INVALID;
   if (d->collision < 0 || d->collision > 3) return LBM_ERR_INVALID;
   if (d->force_kind < 0 || d->force_kind > 3) return LBM_ERR_INVALID;
   if (d->nbc < 0 || d->nbc > LBM_MAX_BC || (d->nbc > 0 && !d->bcs)) return LBM_ERR_INVALID;
@@ -265,7 +270,8 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   c->nx = d->nx;
   c->ny = d->ny;
   c->n = d->nx * d->ny;
-  c->elem = d->storage == LBM_STORE_F64 ? 8 : d->storage == LBM_STORE_F32_DEV ? 4 : 2;
+  c->elem = (d->storage == LBM_STORE_F64 || d->storage == LBM_STORE_DF64_DEV) ? 8
+            : d->storage == LBM_STORE_F32_DEV ? 4 : 2;
 
   for (int b = 0; b < d->nbc; ++b) {
     const lbm_bc& s = d->bcs[b];
@@ -285,9 +291,9 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   p.nx = (int)d->nx;
   p.ny = (int)d->ny;
   p.n = c->n;
-  for (int dd = -3; dd <= 3; ++dd) {
-    p.dxm[dd + 3] = (int)(((dd % d->nx) + d->nx) % d->nx);
-    p.dym[dd + 3] = (int)(((dd % d->ny) + d->ny) % d->ny);
+  for (int s = -3; s <= 3; ++s) {
+    p.dxm[s + 3] = (int)(((s % d->nx) + d->nx) % d->nx);
+    p.dym[s + 3] = (int)(((s % d->ny) + d->ny) % d->ny);
   }
   for (int i = 0; i < LBM_MAX_Q; ++i) p.w[i] = i < c->Q ? d->weights[i] : 0.0;
   p.cs = d->speed_of_sound_squared;
@@ -307,6 +313,17 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
     }
     p.shift = tau[1];
   }
+  if (c->coll == LBM_SRT || c->coll == LBM_ITERATIVE_INIT) {
+    p.pom_s = p.pom_a = 1 / tau[0];
+    p.pa_s = p.pa_a = (1 - 1 / tau[0]) / 2;
+  } else if (c->coll == LBM_TRT) {
+    p.pom_s = 1 / tau[0];
+    p.pom_a = 1 / tau[1];
+    p.pa_s = (1 - 1 / tau[0]) / 2;
+    p.pa_a = (1 - 1 / tau[1]) / 2;
+  }
+  p.hcs = p.cs / 2;
+  p.hcs2 = p.cs * p.cs / 2;
   p.force_kind = d->force_kind;
   p.F[0] = d->force[0];
   p.F[1] = d->force[1];
@@ -348,6 +365,12 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   q.inv_ts = (float)p.inv_ts;
   q.inv_ta = (float)p.inv_ta;
   q.shift = (float)p.shift;
+  q.pa_s = (float)p.pa_s;
+  q.pa_a = (float)p.pa_a;
+  q.pom_s = (float)p.pom_s;
+  q.pom_a = (float)p.pom_a;
+  q.hcs = (float)p.hcs;
+  q.hcs2 = (float)p.hcs2;
   for (int k = 0; k < 4; ++k) {
     q.mrt_a[k] = (float)p.mrt_a[k];
     q.mrt_b[k] = (float)p.mrt_b[k];
@@ -358,6 +381,82 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   for (int k = 0; k < 6; ++k) q.shear[k] = p.shear[k];
   q.nbc = p.nbc;
   for (int b = 0; b < p.nbc; ++b) q.bc[b] = p.bc[b];
+  // First-order equilibrium coefficients of the deviation storages, w1_i = (1/c_s²) w_i.  The
+  // equilibrium's momentum is (Σ_i w1_i c_i c_i)·ρu; with w1 rounded to FP32 the second moment is
+  // 1 + O(1e-8), and the relaxation turns that into a momentum drift that grows linearly in time.
+  // So one velocity class (of nonzero weight) absorbs the rounding: its coefficient is solved
+  // from Σ_i w1_i c_ix² = 1 over the already-rounded others, and the class whose solution is
+  // representable exactly is preferred (D2Q4/5/9/13: exact; D2Q17/37: residual ~1e-10).
+  {
+    for (int i = 0; i < LBM_MAX_Q; ++i) p.w1[i] = i < c->Q ? p.cs * p.w[i] : 0.0;
+    float w1f[LBM_MAX_Q];
+    for (int i = 0; i < LBM_MAX_Q; ++i) w1f[i] = (float)p.w1[i];
+    long double best_res = -1.0L;
+    float best_val = 0.f;
+    int best_cls = -1;
+    for (int i = 0; i < c->Q; ++i) {  // candidate class: the velocities with i's (|cx|, |cy|) set
+      const int a = std::abs(c->lat.cx[i]), b = std::abs(c->lat.cy[i]);
+      const int lo_ab = std::min(a, b), hi_ab = std::max(a, b);
+      if (p.w[i] == 0.0) continue;
+      long double other = 0.0L, c2 = 0.0L;
+      for (int j = 0; j < c->Q; ++j) {
+        const int aj = std::abs(c->lat.cx[j]), bj = std::abs(c->lat.cy[j]);
+        const long double cx2 = (long double)(c->lat.cx[j] * c->lat.cx[j]);
+        if (std::min(aj, bj) == lo_ab && std::max(aj, bj) == hi_ab) c2 += cx2;
+        else other += (long double)w1f[j] * cx2;
+      }
+      if (c2 == 0.0L) continue;
+      const float val = (float)((1.0L - other) / c2);
+      long double res = 1.0L - other - (long double)val * c2;
+      if (res < 0) res = -res;
+      if (best_cls < 0 || res < best_res) {
+        best_res = res;
+        best_val = val;
+        best_cls = i;
+      }
+    }
+    if (best_cls >= 0) {
+      const int a = std::abs(c->lat.cx[best_cls]), b = std::abs(c->lat.cy[best_cls]);
+      for (int j = 0; j < c->Q; ++j) {
+        const int aj = std::abs(c->lat.cx[j]), bj = std::abs(c->lat.cy[j]);
+        if (std::min(aj, bj) == std::min(a, b) && std::max(aj, bj) == std::max(a, b)) w1f[j] = best_val;
+      }
+    }
+    for (int i = 0; i < LBM_MAX_Q; ++i) q.w1[i] = w1f[i];
+  }
+  // float-float copy (every constant split once on the host)
+  StepParams<dd>& x = c->px;
+  x.nx = p.nx;
+  x.ny = p.ny;
+  x.n = p.n;
+  for (int k = 0; k < 7; ++k) {
+    x.dxm[k] = p.dxm[k];
+    x.dym[k] = p.dym[k];
+  }
+  for (int i = 0; i < LBM_MAX_Q; ++i) x.w[i] = dd(p.w[i]);
+  for (int i = 0; i < LBM_MAX_Q; ++i) x.w1[i] = dd(p.w1[i]);
+  x.cs = dd(p.cs);
+  x.om_a = dd(p.om_a);
+  x.om_b = dd(p.om_b);
+  x.inv_ts = dd(p.inv_ts);
+  x.inv_ta = dd(p.inv_ta);
+  x.shift = dd(p.shift);
+  x.pa_s = dd(p.pa_s);
+  x.pa_a = dd(p.pa_a);
+  x.pom_s = dd(p.pom_s);
+  x.pom_a = dd(p.pom_a);
+  x.hcs = dd(p.hcs);
+  x.hcs2 = dd(p.hcs2);
+  for (int k = 0; k < 4; ++k) {
+    x.mrt_a[k] = dd(p.mrt_a[k]);
+    x.mrt_b[k] = dd(p.mrt_b[k]);
+  }
+  x.force_kind = p.force_kind;
+  x.F[0] = dd(p.F[0]);
+  x.F[1] = dd(p.F[1]);
+  for (int k = 0; k < 6; ++k) x.shear[k] = p.shear[k];
+  x.nbc = p.nbc;
+  for (int b = 0; b < p.nbc; ++b) x.bc[b] = p.bc[b];
 
   // reduction constants
   for (int i = 0; i < LBM_MAX_Q; ++i) c->red.w[i] = p.w[i];
@@ -411,6 +510,14 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
         lbm_destroy(c);
         return LBM_ERR_NOMEM;
       }
+    } else if (c->storage == LBM_STORE_DF64_DEV) {
+      std::vector<dd> tmp(cnt);
+      for (size_t k = 0; k < cnt; ++k) tmp[k] = dd(d->nonlinear[k]);
+      if (cudaMalloc(&c->d_nonlinear, cnt * sizeof(dd)) != cudaSuccess ||
+          cudaMemcpy(c->d_nonlinear, tmp.data(), cnt * sizeof(dd), cudaMemcpyHostToDevice) != cudaSuccess) {
+        lbm_destroy(c);
+        return LBM_ERR_NOMEM;
+      }
     } else {
       std::vector<float> tmp(cnt);
       for (size_t k = 0; k < cnt; ++k) tmp[k] = (float)d->nonlinear[k];
@@ -421,9 +528,10 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
       }
     }
   }
-  p.Ffield = q.Ffield = c->d_force;
-  p.xr = q.xr = c->d_xr;
-  p.yr = q.yr = c->d_yr;
+  p.Ffield = q.Ffield = x.Ffield = c->d_force;
+  p.xr = q.xr = x.xr = c->d_xr;
+  p.yr = q.yr = x.yr = c->d_yr;
+  x.nonlinear = static_cast<const dd*>(c->d_nonlinear);
   p.nonlinear = static_cast<const double*>(c->d_nonlinear);
   q.nonlinear = static_cast<const float*>(c->d_nonlinear);
   *out = c;

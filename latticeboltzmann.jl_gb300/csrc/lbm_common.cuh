@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "../../include/lbm_gb300.h"
+#include "lbm_df64.cuh"
 
 namespace lbm {
 
@@ -89,6 +90,18 @@ struct F16Dev {
   __device__ __forceinline__ static void st(T* p, C v) { *p = __float2half_rn(v); }
 };
 
+struct DF64Dev {
+  using T = float2;
+  using C = dd;
+  static constexpr bool DEV = true;
+  static constexpr int id = LBM_STORE_DF64_DEV;
+  __device__ __forceinline__ static C ld(const T* p) {
+    const float2 v = __ldg(p);
+    return dd(v.x, v.y);
+  }
+  __device__ __forceinline__ static void st(T* p, C v) { *p = make_float2(v.hi, v.lo); }
+};
+
 // ---------------------------------------------------------------------------------------
 // Kernel parameter blocks (passed by value; they live in the constant bank).
 // ---------------------------------------------------------------------------------------
@@ -108,6 +121,10 @@ struct StepParams {
   CT om_a, om_b;               // SRT: (1 - 1/τ), 1/τ ; ITER: same
   CT inv_ts, inv_ta;           // TRT: 1/τ_s, 1/τ_a
   CT shift;                    // force velocity shift: τ (SRT), τ_a (TRT), τs[2] (MRT)
+  CT pa_s, pa_a, pom_s, pom_a; // pair form: (1 - ω_s)/2, (1 - ω_a)/2, ω_s, ω_a (SRT: ω_s = ω_a = 1/τ)
+  CT hcs, hcs2;                // pair form: (1/c_s²)/2, (1/c_s²)²/2
+  CT w1[LBM_MAX_Q];            // deviation storage: first-order equilibrium coefficients (1/c_s²)·w_i,
+                               // chosen so that Σ_i w1_i c_ix² = 1 holds for the values as stored
   CT mrt_a[4], mrt_b[4];       // MRT: (1 - 1/τ_n), 1/τ_n for n = 1..4
   int force_kind;
   CT F[2];                     // CONSTANT force

@@ -26,6 +26,7 @@ struct OpArgs {
   void* dst = nullptr;
   const StepParams<double>* pd = nullptr;
   const StepParams<float>* pf = nullptr;
+  const StepParams<dd>* px = nullptr;
   const ReduceArgs* red = nullptr;
   int red_k = 0;
   double* partial = nullptr;
@@ -137,6 +138,7 @@ cudaError_t run_op(const OpArgs& a) {
     case LBM_STORE_F64: return run_op_s<L, F64>(a, *a.pd);
     case LBM_STORE_F32_DEV: return run_op_s<L, F32Dev>(a, *a.pf);
     case LBM_STORE_F16_DEV: return run_op_s<L, F16Dev>(a, *a.pf);
+    case LBM_STORE_DF64_DEV: return run_op_s<L, DF64Dev>(a, *a.px);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -49,7 +49,7 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
   pull_offsets<L>(p, x, y, xw, yo);
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) {
-    const int idx = yo[L::R - L::cy(i)] + xw[L::R - L::cx(i)];
+    const int idx = yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)];
     f[i] = S::ld(src + (size_t)i * p.n + idx);
   }
   if (p.nbc > 0 &&
@@ -112,15 +112,14 @@ __device__ __forceinline__ void node_force(const StepParams<CT>& p, int x, int y
 // (D2Q17/21), fourth (D2Q37).  Returns the bracket 1 + a1 + a2/2 [+ a3/6 + a4/24] minus 1,
 // so that feq_i = ρ w_i (1 + P_i).
 template <class L, class CT>
-__device__ __forceinline__ CT eq_poly(CT cs, CT cu, CT usq) {
-  const CT a1 = cs * cu;
+__device__ __forceinline__ CT eq_poly_hi(CT cs, CT cu, CT usq) {  // the terms of order >= 2
   if constexpr (L::EQ == 1) {
-    return a1;
+    return (CT)0;
   } else {
     const CT cs2 = cs * cs;
     const CT cu2 = cu * cu;
     const CT a2 = cs2 * cu2 - cs * usq;
-    CT r = a1 + (CT)0.5 * a2;
+    CT r = (CT)0.5 * a2;
     if constexpr (L::EQ >= 3) {
       const CT a3 = (cs * cu) * (cs2 * cu2 - ((CT)3 * cs) * usq);
       r += (CT)(1.0 / 6.0) * a3;
@@ -131,6 +130,13 @@ __device__ __forceinline__ CT eq_poly(CT cs, CT cu, CT usq) {
     }
     return r;
   }
+}
+
+template <class L, class CT>
+__device__ __forceinline__ CT eq_poly(CT cs, CT cu, CT usq) {
+  const CT a1 = cs * cu;
+  if constexpr (L::EQ == 1) return a1;
+  else return a1 + eq_poly_hi<L>(cs, cu, usq);
 }
 
 // Raw moments M_ab = Σ_i v_i cx_i^a cy_i^b, a + b <= 4, in the order
@@ -183,6 +189,7 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
   B[0] = M[0];  // ρ, or ρ - 1 in deviation form
   B[1] = cs * rho * ux;
   B[2] = cs * rho * uy;
+  CT B1p = rho * ux, B2p = rho * uy;  // deviation storage: first-order coefficients per w1 = cs w
   if constexpr (L::HN >= 2) {
     const CT a = p.mrt_a[1], b = p.mrt_b[1];
     const CT Axx = a * (M[3] - ics * M[0]) + b * (rho * ux * ux);
@@ -207,6 +214,8 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
     B[9] += c3 * Ayyy;
     B[1] -= c3 * (CT)3 * ics * (Axxx + Axyy);
     B[2] -= c3 * (CT)3 * ics * (Axxy + Ayyy);
+    B1p -= c3 * (CT)3 * ics * ics * (Axxx + Axyy);
+    B2p -= c3 * (CT)3 * ics * ics * (Axxy + Ayyy);
   }
   if constexpr (L::HN >= 4) {
     const CT a = p.mrt_a[3], b = p.mrt_b[3];
@@ -227,17 +236,97 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
     B[5] -= c4 * ics * (CT)6 * (Axxyy + Ayyyy);
     B[0] += c4 * ics2 * ((CT)3 * Axxxx + (CT)6 * Axxyy + (CT)3 * Ayyyy);
   }
+  // Deviation storage: the first-order monomials carry w1_i / cs instead of w_i (see collide_node)
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) {
     CT s = B[0];
 #pragma unroll
-    for (int k = 1; k < NM; ++k) {
+    for (int k = DEV ? 3 : 1; k < NM; ++k) {
       const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
       if (coef == 1) s += B[k];
       else if (coef == -1) s -= B[k];
       else if (coef != 0) s += (CT)coef * B[k];
     }
-    v[i] = p.w[i] * s;
+    if constexpr (DEV) {
+      CT s1 = 0;
+      if (L::cx(i) != 0) s1 += (CT)L::cx(i) * B1p;
+      if (L::cy(i) != 0) s1 += (CT)L::cy(i) * B2p;
+      v[i] = p.w[i] * s + p.w1[i] * s1;
+    } else {
+      v[i] = p.w[i] * s;
+    }
+  }
+  (void)B1p;
+  (void)B2p;
+}
+
+// SRT / TRT in deviation storage for velocity sets whose equilibrium is of order <= 2 (D2Q4,
+// D2Q5, D2Q9, D2Q13), in "pair form".  Opposite populations enter only through their sum s and
+// difference d, which give both the moments (δρ = Σ s, j = Σ c d) and the TRT symmetric /
+// antisymmetric parts; the equilibrium is built from j' = ρ(u + τF) directly:
+//   feq_i = S + A,  feq_opp(i) = S - A,
+//   S = w δρ + w ((c²/2)(c_i·j')² - (c/2)|j'|²) / ρ,   A = w1 (c_i·j'),   c = 1/c_s²,
+// and the update is f'_i = Ys + Ya, f'_opp = Ys - Ya with Ys = (1 - ω_s) s/2 + ω_s S,
+// Ya = (1 - ω_a) d/2 + ω_a A (srt.jl:18-62 and trt.jl:42-97 rewritten; SRT is ω_s = ω_a).
+template <class L, class CT>
+__device__ __forceinline__ void collide_pairs_dev(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
+  CT sp[L::Q], dp[L::Q];
+  CT drho = 0;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) {
+    const int o = L::opp(i);
+    if (o == i) {
+      drho += v[i];
+    } else if (o > i) {
+      sp[i] = v[i] + v[o];
+      dp[i] = v[i] - v[o];
+      drho += sp[i];
+    }
+  }
+  CT jx = 0, jy = 0;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) {
+    const int o = L::opp(i);
+    if (o <= i) continue;
+    if (L::cx(i) == 1) jx += dp[i];
+    else if (L::cx(i) == -1) jx -= dp[i];
+    else if (L::cx(i) != 0) jx += (CT)L::cx(i) * dp[i];
+    if (L::cy(i) == 1) jy += dp[i];
+    else if (L::cy(i) == -1) jy -= dp[i];
+    else if (L::cy(i) != 0) jy += (CT)L::cy(i) * dp[i];
+  }
+  const CT rho = (CT)1 + drho;
+  const CT inv = (CT)1 / rho;
+  if (has_force) {  // j' = ρ (u + τ F)
+    const CT rs = rho * p.shift;
+    jx += rs * Fx;
+    jy += rs * Fy;
+  }
+  CT q2 = 0;
+  if constexpr (L::EQ >= 2) q2 = (p.hcs * (jx * jx + jy * jy)) * inv;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) {
+    const int o = L::opp(i);
+    if (o == i) {
+      CT S = p.w[i] * drho;
+      if constexpr (L::EQ >= 2) S -= p.w[i] * q2;
+      v[i] = ((CT)2 * p.pa_s) * v[i] + p.pom_s * S;
+    } else if (o > i) {
+      CT X = 0;
+      if (L::cx(i) == 1) X += jx;
+      else if (L::cx(i) == -1) X -= jx;
+      else if (L::cx(i) != 0) X += (CT)L::cx(i) * jx;
+      if (L::cy(i) == 1) X += jy;
+      else if (L::cy(i) == -1) X -= jy;
+      else if (L::cy(i) != 0) X += (CT)L::cy(i) * jy;
+      CT S = p.w[i] * drho;
+      if constexpr (L::EQ >= 2) S += p.w[i] * ((p.hcs2 * (X * X)) * inv - q2);
+      const CT A = p.w1[i] * X;
+      const CT Ys = p.pa_s * sp[i] + p.pom_s * S;
+      const CT Ya = p.pa_a * dp[i] + p.pom_a * A;
+      v[i] = Ys + Ya;
+      v[o] = Ys - Ya;
+    }
   }
 }
 
@@ -254,6 +343,9 @@ __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int
   if (COLL != LBM_ITERATIVE_INIT && has_force) node_force(p, x, y, Fx, Fy);
   if constexpr (COLL == LBM_MRT) {
     mrt_collide<L, DEV>(p, v, Fx, Fy, has_force);
+    return;
+  } else if constexpr (DEV && L::EQ <= 2 && (COLL == LBM_SRT || COLL == LBM_TRT)) {
+    collide_pairs_dev<L>(p, v, Fx, Fy, has_force);
     return;
   } else {
     CT s = v[0];
@@ -298,9 +390,16 @@ __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int
         if (L::cy(i) == 1) cu += uy;
         else if (L::cy(i) == -1) cu -= uy;
         else if (L::cy(i) != 0) cu += (CT)L::cy(i) * uy;
-        const CT P = eq_poly<L>(p.cs, cu, usq);
-        // F64: feq = ρ w (1 + P);  deviation: geq = feq - w = w (δρ + ρ P)
-        feq[i] = DEV ? p.w[i] * (drho + rho * P) : (rho * p.w[i]) * ((CT)1 + P);
+        // F64: feq = ρ w (1 + P) as the reference forms it.  Deviation storage: geq = feq - w =
+        // w δρ + ρ (w1 c·u + w P_{>=2}), with w1 the first-order coefficients whose second moment
+        // is exactly 1 in the stored precision, so the equilibrium carries exactly the momentum ρu
+        // (rounded weights would give K ρu with K - 1 ~ 1e-8 in FP32, a drift growing with time).
+        if constexpr (DEV) {
+          feq[i] = p.w[i] * drho + rho * (p.w1[i] * cu + p.w[i] * eq_poly_hi<L>(p.cs, cu, usq));
+        } else {
+          const CT P = eq_poly<L>(p.cs, cu, usq);
+          feq[i] = (rho * p.w[i]) * ((CT)1 + P);
+        }
       }
       if constexpr (COLL == LBM_SRT) {
 #pragma unroll

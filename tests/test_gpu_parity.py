@@ -52,19 +52,24 @@ def _run_pair(lbm, O, qname, nx, ny, coll, taus, steps, bcs_spec=(), force=None,
     return f_gpu, f_ref
 
 
+STORAGES = ["f64", "df64dev"]  # the FP64-class storages: both held to the 1e-12 bound
+
+
+@pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("qname", QUADS)
 @pytest.mark.parametrize("coll,taus", [("SRT", [0.8]), ("TRT", [0.7, 1.1]), ("MRT", [0.9, 0.75, 1.2, 0.6])])
-def test_periodic(lbm_gpu, O, qname, coll, taus):
-    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, 37, 21, coll, taus, 25)
+def test_periodic(lbm_gpu, O, qname, coll, taus, storage):
+    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, 37, 21, coll, taus, 25, storage=storage)
     assert rel_err(f_gpu, f_ref) <= TOL
 
 
+@pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("qname", QUADS)
 @pytest.mark.parametrize("shape", [(1, 1), (2, 3), (5, 4), (130, 3)])
-def test_small_and_ragged_lattices(lbm_gpu, O, qname, shape):
+def test_small_and_ragged_lattices(lbm_gpu, O, qname, shape, storage):
     """Lattices smaller than the velocity set's reach (periodic wrap of |c| = 3 on a 1 x 1
     lattice, the reference's multispeed regression) and more than one x block."""
-    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, shape[0], shape[1], "TRT", [0.8, 0.9], 7)
+    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, shape[0], shape[1], "TRT", [0.8, 0.9], 7, storage=storage)
     assert rel_err(f_gpu, f_ref) <= TOL
 
 
@@ -79,21 +84,24 @@ PARTIAL = [("bounce_back", "north", (3, 11), (14, 16), (0.0, 0.0)),
            ("bounce_back", "south", (1, 19), (1, 1), (0.0, 0.0))]
 
 
+@pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("qname", QUADS)
 @pytest.mark.parametrize("bcs", [WALLS, CAVITY, PARTIAL], ids=["walls", "cavity", "partial"])
 @pytest.mark.parametrize("coll,taus", [("SRT", [0.9]), ("TRT", [0.8, 1.05]), ("MRT", [0.8, 0.8, 0.8, 0.8])])
-def test_boundaries(lbm_gpu, O, qname, bcs, coll, taus):
-    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, 19, 16, coll, taus, 20, bcs_spec=bcs)
+def test_boundaries(lbm_gpu, O, qname, bcs, coll, taus, storage):
+    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, 19, 16, coll, taus, 20, bcs_spec=bcs, storage=storage)
     assert rel_err(f_gpu, f_ref) <= TOL
 
 
+@pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("qname", ["D2Q9", "D2Q17", "D2Q37"])
 @pytest.mark.parametrize("force", ["constant", "field", "shear"])
 @pytest.mark.parametrize("coll,taus", [("SRT", [0.8]), ("TRT", [0.8, 0.95]), ("MRT", [0.7, 0.9, 0.7, 0.7])])
-def test_forces(lbm_gpu, O, qname, force, coll, taus):
+def test_forces(lbm_gpu, O, qname, force, coll, taus, storage):
     bcs = WALLS if force == "constant" else ()
     nx, ny = (19, 16) if force == "constant" else (16, 16)
-    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, nx, ny, coll, taus, 20, bcs_spec=bcs, force=force)
+    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, nx, ny, coll, taus, 20, bcs_spec=bcs, force=force,
+                             storage=storage)
     assert rel_err(f_gpu, f_ref) <= TOL
 
 

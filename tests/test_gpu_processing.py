@@ -52,8 +52,11 @@ def test_taylor_green_config_against_oracle(lbm_gpu, O):
     for mine, key in [(row.error_ρ, "error_rho"), (row.error_u, "error_u"), (row.error_p, "error_p"),
                       (row.error_σ_xx, "error_sigma_xx"), (row.error_σ_xy, "error_sigma_xy")]:
         assert mine == pytest.approx(ref[key], rel=1e-7), key
-    for mine, key in [(row.mass, "mass"), (row.momentum, "momentum"), (row.energy, "energy")]:
-        assert mine == pytest.approx(ref[key], rel=1e-9, abs=1e-14), key
+    # mass and energy are O(1) sums; the total momentum is zero by symmetry up to rounding
+    # noise (~1e-14 on 4096 nodes), compared on the scale of the mass
+    assert row.mass == pytest.approx(ref["mass"], rel=1e-12)
+    assert row.energy == pytest.approx(ref["energy"], rel=1e-9)
+    assert abs(row.momentum - ref["momentum"]) <= 1e-12 * ref["mass"]
     m.close()
 
 
