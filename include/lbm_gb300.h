@@ -203,6 +203,35 @@ int32_t lbm_collide_device(lbm_ctx* ctx, const double* f_in, double* f_out, doub
 int32_t lbm_stream_device(lbm_ctx* ctx, const double* f, double* f_new);                   /* stream!(q, f, f_new), periodic */
 int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old);            /* apply!(bcs, q, f_new, f_old) */
 
+/* ---- reductions without allocation --------------------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot allocate device memory
+ * -- code running while a CUDA graph is being captured, inside another library's stream
+ * callback, or in a host whose device memory belongs to a pool it may not grow -- and that
+ * already hold the populations on the device.  lbm_reduce needs a context, and creating one
+ * allocates; this entry point allocates nothing (no cudaMalloc, cudaFree or allocating
+ * library call).
+ *
+ * It computes the same sums as lbm_reduce for kind TRACK_ERRORS (out[0..15]), COMPARE
+ * (out[0..11]), MEAN_VELOCITY (out[0..1]) or CONSERVED (out[0..3]); other kinds return
+ * LBM_ERR_UNSUPPORTED.  Caller-owned inputs and outputs:
+ *   f         device array of nx*ny*Q doubles, Julia layout, the observed state (f_stream)
+ *   weights   host array of the Q weights, read during the call
+ *   analytic  for TRACK_ERRORS / COMPARE: device pointers (on_device = 1) to the analytic fields
+ *   out       device array of at least 16 doubles, written asynchronously on `stream`
+ *   stream    a cudaStream_t, or NULL for the default stream
+ * Scratch: one partial sum per block (at most 608 blocks x 16 sums) in a fixed 77,824-byte
+ * static device array, held by every GPU that loads the library until the process exits.  Any
+ * lattice below 2^31 nodes fits (larger ones are rejected with LBM_ERR_INVALID), because the
+ * grid never exceeds 608 blocks.  Every call reuses that array and keeps the previous call's
+ * partial sums in it; a call writes every slot it reads, so nothing needs clearing -- but calls
+ * that overlap on the GPU (different streams, or different host threads on one device) race on
+ * it: serialise them.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture.  Returns LBM_OK after the launch; read `out` after synchronising `stream`. */
+int32_t lbm_reduce_noalloc(int32_t quadrature, const double* weights, double speed_of_sound_squared, int64_t nx,
+                           int64_t ny, const double* f, int32_t kind, const lbm_analytic* analytic, double* out,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif
