@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -187,6 +188,90 @@ def cpu_baseline(tau_s, budget_s=12.0):
                       f"{threads} OpenMP threads, C++ restatement of the reference loop"}
 
 
+def bench_tgv64(torch, lbm, storage="f64"):
+    """Taylor-Green vortex 64 x 64, D2Q9 SRT τ = 0.8, equilibrium + off-equilibrium start, 1000
+    steps, TrackHydrodynamicErrors at step 1000 (the CPU-runnable configuration)."""
+    q = lbm.D2Q9()
+    problem = lbm.TaylorGreenVortex(0.1, 1, 64, 64, static=False)
+    pm = lbm.TrackHydrodynamicErrors(problem, False, 1000)
+    t0 = time.perf_counter()
+    m = lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.SRT, process_method=pm, storage=storage,
+                                  initialization_strategy=lbm.AnalyticalEquilibriumAndOffEquilibrium())
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    lbm.simulate(m, time=range(0, 1000))
+    t2 = time.perf_counter()
+    row = pm.df[-1]
+    m.close()
+    return {"workload": "D2Q9 SRT Taylor-Green vortex 64x64, tau=0.8, 1000 steps, FP64", "storage": storage,
+            "simulate_s": t2 - t1, "setup_s": t1 - t0, "mlups": 64 * 64 * 1000 / (t2 - t1) / 1e6,
+            "error_u": row.error_u, "error_p": row.error_p, "error_sigma_xx": row.error_σ_xx,
+            "error_sigma_xy": row.error_σ_xy}
+
+
+def bench_mrt_d2q37(torch, lbm, steps=500, n=2048):
+    """Regularised MRT D2Q37 shear wave n x n, τ = 0.6, u_x = 0.01 sin(2π y / n), 500 steps:
+    MLUPS, HBM fraction and the velocity / stress errors against the analytic decay."""
+    q = lbm.D2Q37()
+    tau = 0.6
+    problem = lbm.ShearWave(n, n, (tau - 0.5) / q.speed_of_sound_squared, 0.01)
+    f0 = lbm.initialize(lbm.AnalyticalEquilibrium(), q, problem)
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    out = {"workload": f"D2Q37 regularised MRT shear wave {n}x{n}, tau=0.6, {steps} steps"}
+    for storage, esize in (("f64", 8), ("df64dev", 8), ("f32dev", 4)):
+        m = lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.MRT(q, tau), storage=storage, f0=f0)
+        st = steps if storage != "f64" else max(20, steps // 10)
+        sec, _ = time_device(torch, m, st, 3, 1.0)
+        row = lbm.track_errors(m, problem, st + 3)
+        m.close()
+        mlups = n * n * st / sec / 1e6
+        out[storage] = {"mlups": mlups, "steps_timed": st, "hbm_frac": 2 * 37 * esize * mlups * 1e6 / 1e9 / peak,
+                        "error_u": row.error_u, "error_sigma_xy": row.error_σ_xy}
+    return out
+
+
+def bench_batched(torch, lbm):
+    res = lbm.run_tgv_study(storage="df64dev", torch=torch)
+    res.pop("errors", None)
+    res["workload"] = ("48 Taylor-Green lattices N in {16..1024}^2 x {D2Q9, D2Q17}, tau ~ U[0.51, 2.0] (seeded), "
+                       "steps = N^2/256, float-float storage, one CUDA graph vs one lattice after another")
+    return res
+
+
+def bench_adjoint(torch, lbm, n=512, steps=4000):
+    q = lbm.D2Q9()
+    tau_s = 0.8
+    out = {"workload": f"adjoint of D2Q9 TRT {n}x{n} periodic, {steps} steps, loss = |u_T - u*|^2, "
+                       "divergence-free Fourier start (k <= 8, amplitude 0.01), sqrt(T) checkpointing"}
+    u0 = lbm.divergence_free_field(n, n, 8, 0.01, seed=11)
+    ut = lbm.divergence_free_field(n, n, 8, 0.01, seed=12)
+    for st in ("f32dev",):
+        prob = lbm.AdjointProblem(q, n, n, lbm.TRT.fields(tau_s, lbm.trt_magic(tau_s)), force=(1e-6, 0.0),
+                                  nsteps=steps, storage=st)
+        prob.run(u0, ut, want_grad_u0=False)  # captures the graph
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = prob.run(u0, ut)
+        t1 = time.perf_counter()
+        prob.close()
+        out[st] = {"seconds": t1 - t0, "forward_equivalent_mlups": n * n * steps / (t1 - t0) / 1e6,
+                   "loss": res["loss"], "dL_dtau_s_total": lbm.magic_total_derivative(res, tau_s),
+                   "dL_dF": [float(x) for x in res["dF"]]}
+    return out
+
+
+def finite(obj):
+    """The JSON line carries no NaN / Infinity tokens (they are not JSON): such values become null."""
+    if isinstance(obj, float):
+        return obj if math.isfinite(obj) else None
+    if isinstance(obj, dict):
+        return {k: finite(v) for k, v in obj.items()}
+    if isinstance(obj, (list, tuple)):
+        return [finite(v) for v in obj]
+    return obj
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -210,7 +295,7 @@ def run_reference(args):
                                    "not runnable on the box)", "nx": NX, "ny": NY, "tau_s": tau_s},
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    print(json.dumps(finite(line), allow_nan=False))
     return 0
 
 
@@ -224,6 +309,8 @@ def main():
     ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev"])
     ap.add_argument("--profile", action="store_true",
                     help="time only the device loop of the chosen storage (for profiler runs)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the other configurations (Taylor-Green 64^2, D2Q37 MRT, batched study, adjoint)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -277,6 +364,9 @@ def main():
             mx.close()
             extra[st] = {"value": NX * NY * args.steps / sx / 1e6, "unit": "MLUPS", "speedup_vs_f64": seconds / sx,
                          "roofline_frac": BYTES_PER_LU[st] * NX * NY / (sx / args.steps) / 1e9 / peak_gbs}
+    if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
+        extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
+                            "batched": bench_batched(torch, lbm), "adjoint": bench_adjoint(torch, lbm)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(tau_s)
@@ -296,7 +386,7 @@ def main():
                              "bytes_per_lu": bytes_lu, "kernel": "step_kernel<D2Q9,TRT,fused>"},
                 "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu}
         line.update(extra)
-        print(json.dumps(line))
+        print(json.dumps(finite(line), allow_nan=False))
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

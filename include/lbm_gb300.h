@@ -203,6 +203,41 @@ int32_t lbm_collide_device(lbm_ctx* ctx, const double* f_in, double* f_out, doub
 int32_t lbm_stream_device(lbm_ctx* ctx, const double* f, double* f_new);                   /* stream!(q, f, f_new), periodic */
 int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old);            /* apply!(bcs, q, f_new, f_old) */
 
+/* ---- batches: many lattices in one CUDA graph ---------------------------------------------
+ * A convergence study or a parameter sweep is a set of independent lattices (one `simulate` per
+ * point in the reference, e.g. examples/notebooks/taylor_green_vortex.ipynb cell 3 and
+ * examples/notebooks/trt_magic_parameter.ipynb).  A batch groups existing contexts (same
+ * storage, SRT or TRT, velocity sets D2Q4..D2Q17, no time-dependent force) and advances member k
+ * by nsteps[k] steps with ONE graph launch: one kernel per global step, covering every member
+ * still running.  Members keep their buffers; upload / download / reduce them as usual before
+ * and after (their streams are ordered against the batch). */
+typedef struct lbm_batch lbm_batch;
+int32_t lbm_batch_create(lbm_batch** batch, lbm_ctx* const* members, int32_t count);
+void lbm_batch_destroy(lbm_batch* batch);
+int32_t lbm_batch_step(lbm_batch* batch, const int64_t* nsteps);
+int32_t lbm_batch_set_stream(lbm_batch* batch, void* stream);
+int32_t lbm_batch_synchronize(lbm_batch* batch);
+int64_t lbm_batch_last_launch_count(const lbm_batch* batch);
+const char* lbm_batch_last_error(const lbm_batch* batch);
+
+/* ---- adjoint (reverse-mode gradients) -----------------------------------------------------
+ * No differentiation exists in the reference; this is the discrete adjoint of the fused step
+ * for periodic D2Q9 / D2Q13 lattices with SRT or TRT and a uniform force (the context's
+ * descriptor), FP64 or FP32-deviation storage.  For the loss
+ *   L = Σ_x |u(f_T) - u*|²,  f_0 = f_eq(ρ = 1, u0),  f_{t+1} = stream(collide(f_t)),  T = nsteps,
+ * lbm_adjoint_run returns result[0] = L, result[1] = ∂L/∂τ_s (SRT: dL/dτ), result[2] = ∂L/∂τ_a
+ * (TRT; 0 for SRT), result[3..4] = ∂L/∂F, and, if grad_u0 is not NULL, ∂L/∂u0 as two planes of
+ * nx*ny (Julia layout, like u0 and u_target).  Memory is bounded by checkpointing: the state
+ * entering every checkpoint_every-th step is kept (0 selects ⌈√nsteps⌉) and each segment is
+ * recomputed once during the reverse sweep; the whole forward + reverse sweep is one CUDA graph.
+ * Loss and parameter sums are FP64, in a fixed order. */
+typedef struct lbm_adjoint lbm_adjoint;
+int32_t lbm_adjoint_create(lbm_adjoint** adjoint, lbm_ctx* ctx, int64_t nsteps, int64_t checkpoint_every);
+void lbm_adjoint_destroy(lbm_adjoint* adjoint);
+int32_t lbm_adjoint_run(lbm_adjoint* adjoint, const double* u0, const double* u_target, double* result,
+                        double* grad_u0);
+const char* lbm_adjoint_last_error(const lbm_adjoint* adjoint);
+
 /* ---- reductions without allocation --------------------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate device memory
  * -- code running while a CUDA graph is being captured, inside another library's stream

@@ -35,9 +35,11 @@ from .processing_methods import (ProcessingMethod, TrackHydrodynamicErrors, Comp
                                  ProcessIterativeInitialization, TakeSnapshots, NoProcessing, StopCriteriaFor,
                                  NoStoppingCriteria, MeanVelocityStoppingCriteria, VelocityConvergenceStoppingCriteria,
                                  DensityConvergence, TrackRow, CompareRow, track_errors)
-from .device import DeviceLattice
+from .device import DeviceLattice, DeviceBatch
 from .model import LatticeBoltzmannModel, simulate, simulate_model, run_steps, collide, stream, apply
 from . import build_native
+from .studies import tgv_instances, run_tgv_study, convergence_order
+from .adjoint import AdjointProblem, divergence_free_field, trt_magic, magic_total_derivative, LBMLoss
 
 StopCriteria = StopCriteriaFor
 

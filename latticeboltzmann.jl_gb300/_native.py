@@ -107,6 +107,28 @@ def lib():
         L.lbm_stream_device.restype = C.c_int32
         L.lbm_apply_bcs_device.argtypes = [vp, vp, vp]
         L.lbm_apply_bcs_device.restype = C.c_int32
+        L.lbm_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.c_int32]
+        L.lbm_batch_create.restype = C.c_int32
+        L.lbm_batch_destroy.argtypes = [vp]
+        L.lbm_batch_destroy.restype = None
+        L.lbm_batch_step.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.lbm_batch_step.restype = C.c_int32
+        L.lbm_batch_set_stream.argtypes = [vp, vp]
+        L.lbm_batch_set_stream.restype = C.c_int32
+        L.lbm_batch_synchronize.argtypes = [vp]
+        L.lbm_batch_synchronize.restype = C.c_int32
+        L.lbm_batch_last_launch_count.argtypes = [vp]
+        L.lbm_batch_last_launch_count.restype = C.c_int64
+        L.lbm_batch_last_error.argtypes = [vp]
+        L.lbm_batch_last_error.restype = C.c_char_p
+        L.lbm_adjoint_create.argtypes = [C.POINTER(vp), vp, C.c_int64, C.c_int64]
+        L.lbm_adjoint_create.restype = C.c_int32
+        L.lbm_adjoint_destroy.argtypes = [vp]
+        L.lbm_adjoint_destroy.restype = None
+        L.lbm_adjoint_run.argtypes = [vp, _DP, _DP, _DP, _DP]
+        L.lbm_adjoint_run.restype = C.c_int32
+        L.lbm_adjoint_last_error.argtypes = [vp]
+        L.lbm_adjoint_last_error.restype = C.c_char_p
         _lib = L
         return L
 
@@ -115,7 +137,10 @@ EXPORTED_SYMBOLS = [
     "lbm_abi_version", "lbm_status_string", "lbm_create", "lbm_destroy", "lbm_last_error",
     "lbm_set_stream", "lbm_synchronize", "lbm_upload", "lbm_download", "lbm_upload_device",
     "lbm_download_device", "lbm_step", "lbm_last_launch_count", "lbm_reduce", "lbm_macroscopic",
-    "lbm_collide_device", "lbm_stream_device", "lbm_apply_bcs_device",
+    "lbm_collide_device", "lbm_stream_device", "lbm_apply_bcs_device", "lbm_batch_create", "lbm_batch_destroy",
+    "lbm_batch_step", "lbm_batch_set_stream", "lbm_batch_synchronize", "lbm_batch_last_launch_count",
+    "lbm_batch_last_error", "lbm_adjoint_create", "lbm_adjoint_destroy", "lbm_adjoint_run",
+    "lbm_adjoint_last_error",
 ]
 
 

@@ -1,0 +1,236 @@
+// lbm_adjoint.cuh -- reverse-mode (adjoint) kernels of the fused collide-stream step.
+//
+// The reference has no differentiation; this is the discrete adjoint of the forward map the
+// kernels implement, for periodic lattices with SRT or TRT collision and a uniform force:
+//
+//   A_{t+1} = S C(A_t; τ_s, τ_a, F),  A_0 = f_eq(ρ = 1, u0),  L = Σ_x |u(A_T) - u*|²,
+//
+// with S the periodic pull (a permutation) and C the per-node collision.  The adjoint state
+// λ_t = ∂L/∂A_t obeys λ_t = J_C(A_t)^T S^T λ_{t+1}: S^T is the pull in the opposite direction
+// (λ from x + c_i), and J_C^T is applied per node in O(Q):
+//
+//   C(f) = M f + N f_eq(ρ(f), u'(f)),   M = (1-ω_s) P_s + (1-ω_a) P_a,   N = ω_s P_s + ω_a P_a,
+//   J_C^T μ = M μ + (∂f_eq/∂f)^T ν,  ν = N μ,
+//   (∂f_eq/∂f)^T ν |_k = G_ρ + Σ_a G_a (c_ka - u_a) / ρ,
+//   G_ρ = Σ_i ν_i f_eq,i / ρ,   G_a = Σ_i ν_i ∂f_eq,i/∂u'_a,   u' = u + τ_a F,
+//
+// where P_s / P_a are the symmetric / antisymmetric parts over opposite pairs (trt.jl:71-94).
+// Parameter sensitivities accumulate μ^T ∂C/∂θ per node: -Σ μ^s (f - f_eq) for ω_s,
+// -Σ μ^a (f - f_eq) for ω_a, Σ_a G_a F_a for τ_a through the force shift, τ_a G_a for F_a.
+// Sums are FP64, one slot per block, blocks always own the same nodes (deterministic).
+#pragma once
+
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+constexpr int kAdjThreads = 256;
+constexpr int kAdjParams = 5;  // dω_s, dω_a, dτ_a (force shift), dF_x, dF_y
+
+struct AdjArgs {
+  double Fx, Fy;        // uniform lattice force
+  double shift;         // τ (SRT) or τ_a (TRT)
+};
+
+// Equilibrium of one node as the forward kernel forms it, with ∂feq_i/∂u'_a.
+// F64: feq = ρ w (1 + P);  deviation: geq = feq - w = w δρ + ρ (w1 c·u' + w P_2).
+template <class L, class S>
+__device__ __forceinline__ void adj_equilibrium(const StepParams<typename S::C>& p, typename S::C rho,
+                                                typename S::C drho, typename S::C ux, typename S::C uy,
+                                                typename S::C* feq, typename S::C* dfx, typename S::C* dfy) {
+  using CT = typename S::C;
+  const CT cs = p.cs;
+  const CT usq = ux * ux + uy * uy;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) {
+    const CT cxi = (CT)L::cx(i), cyi = (CT)L::cy(i);
+    const CT cu = cxi * ux + cyi * uy;
+    const CT P2 = (CT)0.5 * (cs * cs * cu * cu - cs * usq);
+    if constexpr (S::DEV) {
+      feq[i] = p.w[i] * drho + rho * (p.w1[i] * cu + p.w[i] * P2);
+      dfx[i] = rho * (p.w1[i] * cxi + p.w[i] * (cs * cs * cu * cxi - cs * ux));
+      dfy[i] = rho * (p.w1[i] * cyi + p.w[i] * (cs * cs * cu * cyi - cs * uy));
+    } else {
+      feq[i] = (rho * p.w[i]) * ((CT)1 + cs * cu + P2);
+      dfx[i] = rho * p.w[i] * (cs * cxi + cs * cs * cu * cxi - cs * ux);
+      dfy[i] = rho * p.w[i] * (cs * cyi + cs * cs * cu * cyi - cs * uy);
+    }
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void adj_block_add(double (&acc)[K], double* slots) {
+  __shared__ double sh[kAdjThreads / 32][K];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int wi = 0; wi < kAdjThreads / 32; ++wi) s += sh[wi][threadIdx.x];
+    slots[(size_t)blockIdx.x * K + threadIdx.x] += s;
+  }
+}
+
+// A_0 = f_eq(ρ = 1, u0) in the storage's form.
+template <class L, class S>
+__global__ void __launch_bounds__(kAdjThreads) adj_init_kernel(StepParams<typename S::C> p, const double* __restrict__ u0,
+                                                               typename S::T* __restrict__ a0) {
+  using CT = typename S::C;
+  for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
+       node += (long long)gridDim.x * kAdjThreads) {
+    const CT ux = (CT)u0[node], uy = (CT)u0[p.n + node];
+    CT feq[L::Q], dfx[L::Q], dfy[L::Q];
+    adj_equilibrium<L, S>(p, (CT)1, (CT)0, ux, uy, feq, dfx, dfy);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) S::st(a0 + (size_t)i * p.n + node, feq[i]);
+  }
+}
+
+// Loss L = Σ |u(A_T) - u*|² (FP64) and λ_T = ∂L/∂A_T, with A_T pulled from B_{T-1}.
+template <class L, class S>
+__global__ void __launch_bounds__(kAdjThreads) adj_loss_kernel(StepParams<typename S::C> p, const typename S::T* __restrict__ src,
+                                                               const double* __restrict__ ut, typename S::T* __restrict__ lam,
+                                                               double* __restrict__ slots) {
+  using CT = typename S::C;
+  double acc[1] = {0.0};
+  for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
+       node += (long long)gridDim.x * kAdjThreads) {
+    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+    CT v[L::Q];
+    load_streamed<L, S>(p, src, x, y, v);
+    double rho = 0.0, jx = 0.0, jy = 0.0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const double f = S::DEV ? (double)p.w[i] + (double)v[i] : (double)v[i];
+      rho += f;
+      jx += f * L::cx(i);
+      jy += f * L::cy(i);
+    }
+    const double ux = jx / rho, uy = jy / rho;
+    const double ex = ux - ut[node], ey = uy - ut[p.n + node];
+    acc[0] += ex * ex + ey * ey;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const double g = 2.0 * (ex * (L::cx(i) - ux) + ey * (L::cy(i) - uy)) / rho;
+      lam[(size_t)i * p.n + node] = (typename S::T)g;
+    }
+  }
+  adj_block_add<1>(acc, slots);
+}
+
+// One reverse step: λ_t = J_C(A_t)^T S^T λ_{t+1}.  A_t is pulled from B_{t-1} (pull = true) or
+// read locally (A_0).  Parameter sensitivities are added to this block's slots.
+template <class L, class S, int COLL>
+__global__ void __launch_bounds__(kAdjThreads) adj_step_kernel(StepParams<typename S::C> p, AdjArgs a,
+                                                               const typename S::T* __restrict__ src, int pull,
+                                                               const typename S::T* __restrict__ lam_next,
+                                                               typename S::T* __restrict__ lam_out,
+                                                               double* __restrict__ slots) {
+  using CT = typename S::C;
+  double acc[kAdjParams] = {0, 0, 0, 0, 0};
+  const CT om_s = COLL == LBM_TRT ? p.inv_ts : p.om_b;
+  const CT om_a = COLL == LBM_TRT ? p.inv_ta : p.om_b;
+  for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
+       node += (long long)gridDim.x * kAdjThreads) {
+    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+    // forward state A_t at the node
+    CT f[L::Q];
+    if (pull) load_streamed<L, S>(p, src, x, y, f);
+    else load_local<L, S>(p, src, (int)node, f);
+    // μ = S^T λ_{t+1}: λ from x + c_i (the opposite of the forward pull)
+    CT mu[L::Q];
+    {
+      int xw[2 * L::R + 1], yo[2 * L::R + 1];
+      pull_offsets<L>(p, x, y, xw, yo);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const int idx = yo[L::R - L::cy(i)] + xw[L::R - L::cx(i)];
+        mu[i] = (CT)lam_next[(size_t)i * p.n + idx];
+      }
+    }
+    // moments, equilibrium and its velocity derivatives (as the forward collision forms them)
+    CT s = 0, jx = 0, jy = 0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      s += f[i];
+      jx += (CT)L::cx(i) * f[i];
+      jy += (CT)L::cy(i) * f[i];
+    }
+    const CT rho = S::DEV ? (CT)1 + s : s;
+    const CT drho = s;
+    const CT ux = jx / rho, uy = jy / rho;
+    const CT upx = ux + (CT)a.shift * (CT)a.Fx, upy = uy + (CT)a.shift * (CT)a.Fy;
+    CT feq[L::Q], dfx[L::Q], dfy[L::Q];
+    adj_equilibrium<L, S>(p, rho, drho, upx, upy, feq, dfx, dfy);
+    // ν = N μ and M μ per opposite pair
+    CT nu[L::Q], Mmu[L::Q];
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const int o = L::opp(i);
+      const CT ms = (CT)0.5 * (mu[i] + mu[o]), ma = (CT)0.5 * (mu[i] - mu[o]);
+      nu[i] = om_s * ms + om_a * ma;
+      Mmu[i] = ((CT)1 - om_s) * ms + ((CT)1 - om_a) * ma;
+      const CT fneq = f[i] - feq[i];  // deviation storage: g - geq
+      acc[0] -= (double)(ms * fneq);
+      acc[1] -= (double)(ma * fneq);
+    }
+    CT Grho = 0, Gx = 0, Gy = 0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const CT fe = S::DEV ? feq[i] + p.w[i] : feq[i];
+      Grho += nu[i] * fe;
+      Gx += nu[i] * dfx[i];
+      Gy += nu[i] * dfy[i];
+    }
+    Grho = Grho / rho;
+    acc[2] += (double)Gx * a.Fx + (double)Gy * a.Fy;
+    acc[3] += (double)a.shift * (double)Gx;
+    acc[4] += (double)a.shift * (double)Gy;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const CT l = Mmu[i] + Grho + (Gx * ((CT)L::cx(i) - ux) + Gy * ((CT)L::cy(i) - uy)) / rho;
+      lam_out[(size_t)i * p.n + node] = (typename S::T)l;
+    }
+  }
+  adj_block_add<kAdjParams>(acc, slots);
+}
+
+// ∂L/∂u0 = (∂A_0/∂u0)^T λ_0 per node, FP64 output planes.
+template <class L, class S>
+__global__ void __launch_bounds__(kAdjThreads) adj_u0_kernel(StepParams<typename S::C> p, const double* __restrict__ u0,
+                                                             const typename S::T* __restrict__ lam0,
+                                                             double* __restrict__ grad) {
+  using CT = typename S::C;
+  for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
+       node += (long long)gridDim.x * kAdjThreads) {
+    const CT ux = (CT)u0[node], uy = (CT)u0[p.n + node];
+    CT feq[L::Q], dfx[L::Q], dfy[L::Q];
+    adj_equilibrium<L, S>(p, (CT)1, (CT)0, ux, uy, feq, dfx, dfy);
+    double gx = 0.0, gy = 0.0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const double l = (double)(CT)lam0[(size_t)i * p.n + node];
+      gx += l * (double)dfx[i];
+      gy += l * (double)dfy[i];
+    }
+    grad[node] = gx;
+    grad[p.n + node] = gy;
+  }
+}
+
+template <int K>
+__global__ void adj_finish_kernel(const double* __restrict__ slots, int nblocks, double* __restrict__ out) {
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += slots[(size_t)b * K + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+}  // namespace lbm

@@ -15,8 +15,21 @@
 #include <vector>
 
 #include "lbm_ops.cuh"
+#include "lbm_batch.cuh"
+#include "lbm_adjoint.cuh"
 
 using namespace lbm;
+
+namespace lbm {
+cudaError_t batch_launch(int storage, int coll, int qid, const void* members, int nactive, long long blocks,
+                         long long t, cudaStream_t s);
+size_t batch_member_size(int storage);
+struct AdjArgs;
+cudaError_t adj_launch(int op, int qid, int storage, int coll, const void* params, AdjArgs a, const void* src, int pull,
+                       const void* lam_next, void* lam_out, double* slots, int nblocks, const double* u0,
+                       const double* ut, double* grad, cudaStream_t s);
+cudaError_t adj_finish(const double* slots, int nblocks, int k, double* out, cudaStream_t s);
+}  // namespace lbm
 
 namespace {
 
@@ -787,6 +800,445 @@ int32_t lbm_apply_bcs_device(lbm_ctx* c, double* f_new, const double* f_old) {
   a.src = f_old;
   a.dst = f_new;
   return run(c, a);
+}
+
+
+}  // extern "C"
+
+// ---- batches -------------------------------------------------------------------------------
+
+struct lbm_batch {
+  std::vector<lbm_ctx*> members;
+  int device = 0, storage = 0, coll = 0;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  void* d_members = nullptr;      // device array of BatchMember<CT>
+  void* h_members = nullptr;      // pinned staging copy
+  size_t member_bytes = 0;
+  cudaEvent_t done = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<int64_t> graph_key;  // sorted step counts the graph was captured for
+  std::vector<int> graph_order;
+  int64_t last_launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int bfail(lbm_batch* b, int status, const std::string& msg) {
+  if (b) b->err = msg;
+  return status;
+}
+
+template <class CT>
+void fill_member(BatchMember<CT>& m, const StepParams<CT>& p, lbm_ctx* c, int64_t steps, long long block_start) {
+  m.p = p;
+  m.buf0 = c->buf[0];
+  m.buf1 = c->buf[1];
+  m.qid = c->qid;
+  m.cur0 = c->cur;
+  m.phase0 = c->phase;
+  m.steps = steps;
+  m.block_start = block_start;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count) {
+  if (!out || !members || count < 1 || count > kBatchMax) return LBM_ERR_INVALID;
+  *out = nullptr;
+  const lbm_ctx* c0 = members[0];
+  if (!c0) return LBM_ERR_INVALID;
+  for (int k = 0; k < count; ++k) {
+    const lbm_ctx* c = members[k];
+    if (!c || c->device != c0->device || c->storage != c0->storage || c->coll != c0->coll) return LBM_ERR_INVALID;
+    if (c->qid > LBM_D2Q17) return LBM_ERR_UNSUPPORTED;
+    if (c->coll != LBM_SRT && c->coll != LBM_TRT) return LBM_ERR_UNSUPPORTED;
+    if (c->storage == LBM_STORE_F16_DEV) return LBM_ERR_UNSUPPORTED;
+    if (c->force_kind == LBM_FORCE_SHEAR) return LBM_ERR_UNSUPPORTED;  // time-dependent forces
+  }
+  lbm_batch* b = new lbm_batch();
+  b->members.assign(members, members + count);
+  b->device = c0->device;
+  b->storage = c0->storage;
+  b->coll = c0->coll;
+  b->member_bytes = batch_member_size(b->storage);
+  cudaSetDevice(b->device);
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMalloc(&b->d_members, b->member_bytes * count) != cudaSuccess ||
+      cudaMallocHost(&b->h_members, b->member_bytes * count) != cudaSuccess) {
+    lbm_batch_destroy(b);
+    return LBM_ERR_NOMEM;
+  }
+  b->stream = b->own_stream;
+  *out = b;
+  return LBM_OK;
+}
+
+void lbm_batch_destroy(lbm_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_members);
+  if (b->h_members) cudaFreeHost(b->h_members);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+}
+
+const char* lbm_batch_last_error(const lbm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+int64_t lbm_batch_last_launch_count(const lbm_batch* b) { return b ? b->last_launches : 0; }
+
+int32_t lbm_batch_set_stream(lbm_batch* b, void* stream) {
+  if (!b) return LBM_ERR_INVALID;
+  cudaSetDevice(b->device);
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "stream synchronize");
+  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_key.clear();
+  }
+  return LBM_OK;
+}
+
+int32_t lbm_batch_synchronize(lbm_batch* b) {
+  if (!b) return LBM_ERR_INVALID;
+  cudaSetDevice(b->device);
+  return cudaStreamSynchronize(b->stream) == cudaSuccess ? LBM_OK : bfail(b, LBM_ERR_CUDA, "synchronize");
+}
+
+// Every member k advances nsteps[k] steps.  All members' steps are issued as ONE CUDA graph of
+// kernels, one per global step, each covering every member still running at that step.
+int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
+  if (!b || !nsteps) return LBM_ERR_INVALID;
+  cudaSetDevice(b->device);
+  const int count = (int)b->members.size();
+  for (int k = 0; k < count; ++k) {
+    if (nsteps[k] < 0) return bfail(b, LBM_ERR_INVALID, "negative step count");
+    if (!b->members[k]->have_state) return bfail(b, LBM_ERR_STATE, "member without uploaded state");
+  }
+  // members grouped by velocity set, each group in descending step order: the running set of a
+  // group at global step t is a prefix of it, with block offsets counted within the group
+  std::vector<int> order(count);
+  for (int k = 0; k < count; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    const int qa = b->members[a]->qid, qc = b->members[c]->qid;
+    return qa != qc ? qa < qc : nsteps[a] > nsteps[c];
+  });
+  std::vector<int64_t> key(count);
+  std::vector<long long> start(count, 0), end(count, 0);  // block range of each member in its group
+  std::vector<int> group_begin;  // first rank of each velocity-set group
+  for (int r = 0; r < count; ++r) {
+    const lbm_ctx* c = b->members[order[r]];
+    key[r] = nsteps[order[r]];
+    const bool first = r == 0 || b->members[order[r - 1]]->qid != c->qid;
+    if (first) group_begin.push_back(r);
+    start[r] = first ? 0 : end[r - 1];
+    end[r] = start[r] + (c->n + kBlockX - 1) / kBlockX;
+  }
+  group_begin.push_back(count);
+  int64_t tmax = 0;
+  for (int r = 0; r < count; ++r) tmax = std::max(tmax, key[r]);
+  b->last_launches = 0;
+  if (tmax == 0) return LBM_OK;
+  // the members' own pending work (uploads, reductions) precedes the batch
+  for (lbm_ctx* c : b->members) {
+    if (cudaEventRecord(b->done, c->stream) != cudaSuccess || cudaStreamWaitEvent(b->stream, b->done, 0) != cudaSuccess)
+      return bfail(b, LBM_ERR_CUDA, "ordering member streams");
+  }
+  // member descriptors (parameters, buffers, current parity and phase) for this call
+  char* h = static_cast<char*>(b->h_members);
+  for (int r = 0; r < count; ++r) {
+    lbm_ctx* c = b->members[order[r]];
+    char* slot = h + r * b->member_bytes;
+    if (b->storage == LBM_STORE_F64)
+      fill_member(*reinterpret_cast<BatchMember<double>*>(slot), c->pd, c, key[r], start[r]);
+    else if (b->storage == LBM_STORE_DF64_DEV)
+      fill_member(*reinterpret_cast<BatchMember<dd>*>(slot), c->px, c, key[r], start[r]);
+    else
+      fill_member(*reinterpret_cast<BatchMember<float>*>(slot), c->pf, c, key[r], start[r]);
+  }
+  if (cudaMemcpyAsync(b->d_members, b->h_members, b->member_bytes * count, cudaMemcpyHostToDevice, b->stream) !=
+      cudaSuccess)
+    return bfail(b, LBM_ERR_CUDA, "descriptor upload");
+  if (!b->graph || b->graph_key != key || b->graph_order != order) {
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return bfail(b, LBM_ERR_CUDA, "begin capture");
+    cudaError_t e = cudaSuccess;
+    const int ngroups = (int)group_begin.size() - 1;
+    std::vector<int> nactive(ngroups);
+    for (int gi = 0; gi < ngroups; ++gi) nactive[gi] = group_begin[gi + 1] - group_begin[gi];
+    for (int64_t t = 0; t < tmax && e == cudaSuccess; ++t) {
+      for (int gi = 0; gi < ngroups && e == cudaSuccess; ++gi) {
+        const int g0 = group_begin[gi];
+        while (nactive[gi] > 0 && key[g0 + nactive[gi] - 1] <= t) --nactive[gi];
+        if (nactive[gi] == 0) continue;
+        const char* base = static_cast<const char*>(b->d_members) + (size_t)g0 * b->member_bytes;
+        e = batch_launch(b->storage, b->coll, b->members[order[g0]]->qid, base, nactive[gi],
+                         end[g0 + nactive[gi] - 1], t, b->stream);
+      }
+    }
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return bfail(b, LBM_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      b->graph = nullptr;
+      return bfail(b, LBM_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+    b->graph_key = key;
+    b->graph_order = order;
+  }
+  if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "graph launch");
+  b->last_launches = tmax;
+  // members continue after the batch: advance their parity / phase and order their streams
+  if (cudaEventRecord(b->done, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "event");
+  for (int k = 0; k < count; ++k) {
+    lbm_ctx* c = b->members[k];
+    if (nsteps[k] > 0) {
+      c->cur = (int)((c->cur + nsteps[k]) & 1);
+      c->phase = POST_COLLIDE;
+    }
+    if (cudaStreamWaitEvent(c->stream, b->done, 0) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "member wait");
+  }
+  return LBM_OK;
+}
+
+
+}  // extern "C"
+
+// ---- adjoint -------------------------------------------------------------------------------
+
+struct lbm_adjoint {
+  lbm_ctx* ctx = nullptr;
+  int64_t T = 0, k = 0, nck = 0;
+  size_t bytes = 0;
+  int nblocks = 0;
+  void* a0 = nullptr;
+  void* fwd[2] = {nullptr, nullptr};
+  std::vector<void*> ckpt;  // ckpt[c] = B_{c k - 1}, the state entering step c k (c >= 1)
+  std::vector<void*> seg;   // recomputed B_t inside one segment
+  void* lam[2] = {nullptr, nullptr};
+  double* d_u0 = nullptr;
+  double* d_ut = nullptr;
+  double* d_grad = nullptr;
+  double* d_slots = nullptr;   // loss: nblocks x 1, then parameters: nblocks x 5
+  double* d_out = nullptr;     // loss, dω_s, dω_a, dτ_a(force), dF_x, dF_y
+  double* h_out = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  std::string err;
+};
+
+namespace {
+
+int afail(lbm_adjoint* a, int status, const std::string& msg) {
+  if (a) a->err = msg;
+  return status;
+}
+
+const void* ctx_params(lbm_ctx* c) {
+  return c->storage == LBM_STORE_F64 ? static_cast<const void*>(&c->pd) : static_cast<const void*>(&c->pf);
+}
+
+// The whole forward sweep, the checkpointed reverse sweep and the sensitivity sums.
+cudaError_t adjoint_sequence(lbm_adjoint* a) {
+  lbm_ctx* c = a->ctx;
+  cudaStream_t s = c->stream;
+  const int nb = a->nblocks;
+  AdjArgs args{};
+  args.Fx = c->force_kind == LBM_FORCE_CONSTANT ? c->pd.F[0] : 0.0;
+  args.Fy = c->force_kind == LBM_FORCE_CONSTANT ? c->pd.F[1] : 0.0;
+  args.shift = c->pd.shift;
+  const void* prm = ctx_params(c);
+  double* loss_slots = a->d_slots;
+  double* par_slots = a->d_slots + nb;
+  cudaError_t e = cudaMemsetAsync(a->d_slots, 0, (size_t)nb * (1 + kAdjParams) * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  // A_0
+  e = adj_launch(0, c->qid, c->storage, c->coll, prm, args, nullptr, 0, nullptr, a->a0, nullptr, nb, a->d_u0, nullptr,
+                 nullptr, s);
+  if (e != cudaSuccess) return e;
+  // forward, keeping B_{ck-1} at every segment boundary
+  auto fwd_step = [&](const void* src, void* dst, bool first) {
+    OpArgs o = base_args(c, first ? OP_COLLIDE : OP_FUSED);
+    o.src = src;
+    o.dst = dst;
+    o.stream = s;
+    return kRun[c->qid](o);
+  };
+  for (int64_t t = 0; t < a->T; ++t) {
+    void* dst = a->fwd[t & 1];
+    e = fwd_step(t == 0 ? a->a0 : a->fwd[(t - 1) & 1], dst, t == 0);
+    if (e != cudaSuccess) return e;
+    if ((t + 1) % a->k == 0 && t + 1 < a->T) {
+      e = cudaMemcpyAsync(a->ckpt[(t + 1) / a->k], dst, a->bytes, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  // loss and λ_T from A_T = S(B_{T-1})
+  e = adj_launch(1, c->qid, c->storage, c->coll, prm, args, a->fwd[(a->T - 1) & 1], 1, nullptr, a->lam[a->T & 1],
+                 loss_slots, nb, nullptr, a->d_ut, nullptr, s);
+  if (e != cudaSuccess) return e;
+  // reverse sweep, one segment at a time from the last
+  for (int64_t cc = a->nck - 1; cc >= 0; --cc) {
+    const int64_t t0 = cc * a->k;
+    const int64_t t1 = std::min<int64_t>((cc + 1) * a->k, a->T) - 1;
+    // recompute B_t for t0 <= t < t1 into seg[t - t0]
+    for (int64_t t = t0; t < t1; ++t) {
+      const void* src = (t == 0) ? a->a0 : (t == t0 ? a->ckpt[cc] : a->seg[t - 1 - t0]);
+      e = fwd_step(src, a->seg[t - t0], t == 0);
+      if (e != cudaSuccess) return e;
+    }
+    for (int64_t t = t1; t >= t0; --t) {
+      const void* src;
+      int pull = 1;
+      if (t == 0) {
+        src = a->a0;
+        pull = 0;
+      } else if (t == t0) {
+        src = a->ckpt[cc];
+      } else {
+        src = a->seg[t - 1 - t0];
+      }
+      e = adj_launch(2, c->qid, c->storage, c->coll, prm, args, src, pull, a->lam[(t + 1) & 1], a->lam[t & 1],
+                     par_slots, nb, nullptr, nullptr, nullptr, s);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  e = adj_launch(3, c->qid, c->storage, c->coll, prm, args, nullptr, 0, a->lam[0], nullptr, nullptr, nb, a->d_u0,
+                 nullptr, a->d_grad, s);
+  if (e != cudaSuccess) return e;
+  e = adj_finish(loss_slots, nb, 1, a->d_out, s);
+  if (e != cudaSuccess) return e;
+  return adj_finish(par_slots, nb, kAdjParams, a->d_out + 1, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_t checkpoint_every) {
+  if (!out || !c || nsteps < 1) return LBM_ERR_INVALID;
+  *out = nullptr;
+  if (c->qid != LBM_D2Q9 && c->qid != LBM_D2Q13) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: D2Q9 / D2Q13 only");
+  if (c->coll != LBM_SRT && c->coll != LBM_TRT) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: SRT / TRT only");
+  if (c->storage != LBM_STORE_F64 && c->storage != LBM_STORE_F32_DEV)
+    return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: FP64 or FP32-deviation storage only");
+  if (c->pd.nbc != 0) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: periodic lattices only");
+  if (c->force_kind != LBM_FORCE_NONE && c->force_kind != LBM_FORCE_CONSTANT)
+    return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: uniform force only");
+  cudaSetDevice(c->device);
+  lbm_adjoint* a = new lbm_adjoint();
+  a->ctx = c;
+  a->T = nsteps;
+  int64_t k = checkpoint_every > 0 ? checkpoint_every : (int64_t)std::ceil(std::sqrt((double)nsteps));
+  a->k = std::max<int64_t>(1, std::min<int64_t>(k, nsteps));
+  a->nck = (a->T + a->k - 1) / a->k;
+  a->bytes = (size_t)c->n * c->Q * c->elem;
+  a->nblocks = (int)std::min<int64_t>((c->n + kAdjThreads - 1) / kAdjThreads, 152 * 4);
+  bool ok = cudaMalloc(&a->a0, a->bytes) == cudaSuccess && cudaMalloc(&a->fwd[0], a->bytes) == cudaSuccess &&
+            cudaMalloc(&a->fwd[1], a->bytes) == cudaSuccess && cudaMalloc(&a->lam[0], a->bytes) == cudaSuccess &&
+            cudaMalloc(&a->lam[1], a->bytes) == cudaSuccess &&
+            cudaMalloc(&a->d_u0, (size_t)c->n * 2 * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&a->d_ut, (size_t)c->n * 2 * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&a->d_grad, (size_t)c->n * 2 * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&a->d_slots, (size_t)a->nblocks * (1 + kAdjParams) * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&a->d_out, 8 * sizeof(double)) == cudaSuccess &&
+            cudaMallocHost(&a->h_out, 8 * sizeof(double)) == cudaSuccess;
+  a->ckpt.assign(a->nck, nullptr);
+  for (int64_t cc = 1; ok && cc < a->nck; ++cc) ok = cudaMalloc(&a->ckpt[cc], a->bytes) == cudaSuccess;
+  a->seg.assign(a->k, nullptr);
+  for (int64_t j = 0; ok && j < a->k; ++j) ok = cudaMalloc(&a->seg[j], a->bytes) == cudaSuccess;
+  if (!ok) {
+    lbm_adjoint_destroy(a);
+    return fail(c, LBM_ERR_NOMEM, "adjoint: device memory for checkpoints");
+  }
+  *out = a;
+  return LBM_OK;
+}
+
+void lbm_adjoint_destroy(lbm_adjoint* a) {
+  if (!a) return;
+  cudaSetDevice(a->ctx->device);
+  cudaStreamSynchronize(a->ctx->stream);
+  if (a->graph) cudaGraphExecDestroy(a->graph);
+  void* bufs[] = {a->a0, a->fwd[0], a->fwd[1], a->lam[0], a->lam[1], a->d_u0, a->d_ut, a->d_grad, a->d_slots, a->d_out};
+  for (void* b : bufs) cudaFree(b);
+  for (void* b : a->ckpt) cudaFree(b);
+  for (void* b : a->seg) cudaFree(b);
+  if (a->h_out) cudaFreeHost(a->h_out);
+  delete a;
+}
+
+const char* lbm_adjoint_last_error(const lbm_adjoint* a) { return a ? a->err.c_str() : "null adjoint"; }
+
+int32_t lbm_adjoint_run(lbm_adjoint* a, const double* u0, const double* u_target, double* result,
+                        double* grad_u0) {
+  if (!a || !u0 || !u_target || !result) return LBM_ERR_INVALID;
+  lbm_ctx* c = a->ctx;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const size_t vb = (size_t)c->n * 2 * sizeof(double);
+  if (cudaMemcpyAsync(a->d_u0, u0, vb, cudaMemcpyDefault, s) != cudaSuccess ||
+      cudaMemcpyAsync(a->d_ut, u_target, vb, cudaMemcpyDefault, s) != cudaSuccess)
+    return afail(a, LBM_ERR_CUDA, "adjoint: input copies");
+  if (!a->graph || a->graph_stream != s) {
+    if (a->graph) {
+      cudaGraphExecDestroy(a->graph);
+      a->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return afail(a, LBM_ERR_CUDA, "adjoint: begin capture");
+    cudaError_t e = adjoint_sequence(a);
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return afail(a, LBM_ERR_CUDA, std::string("adjoint capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&a->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      a->graph = nullptr;
+      return afail(a, LBM_ERR_CUDA, std::string("adjoint graph: ") + cudaGetErrorString(e));
+    }
+    a->graph_stream = s;
+  }
+  if (cudaGraphLaunch(a->graph, s) != cudaSuccess) return afail(a, LBM_ERR_CUDA, "adjoint: graph launch");
+  c->last_launches = 3 * a->T;
+  if (cudaMemcpyAsync(a->h_out, a->d_out, 6 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return afail(a, LBM_ERR_CUDA, "adjoint: result copy");
+  if (grad_u0 && cudaMemcpyAsync(grad_u0, a->d_grad, vb, cudaMemcpyDefault, s) != cudaSuccess)
+    return afail(a, LBM_ERR_CUDA, "adjoint: gradient copy");
+  if (cudaStreamSynchronize(s) != cudaSuccess) return afail(a, LBM_ERR_CUDA, "adjoint: synchronize");
+  // result: loss, dL/dτ_s, dL/dτ_a, dL/dF_x, dL/dF_y (partial derivatives; SRT: dL/dτ in [1] and [2] summed)
+  const double* h = a->h_out;
+  const double ts = c->coll == LBM_TRT ? 1.0 / c->pd.inv_ts : 1.0 / c->pd.om_b;
+  const double ta = c->coll == LBM_TRT ? 1.0 / c->pd.inv_ta : ts;
+  result[0] = h[0];
+  if (c->coll == LBM_TRT) {
+    result[1] = h[1] * (-1.0 / (ts * ts));
+    result[2] = h[2] * (-1.0 / (ta * ta)) + h[3];
+  } else {
+    result[1] = (h[1] + h[2]) * (-1.0 / (ts * ts)) + h[3];
+    result[2] = 0.0;
+  }
+  result[3] = h[4];
+  result[4] = h[5];
+  return LBM_OK;
 }
 
 }  // extern "C"

@@ -81,6 +81,34 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
   }
 }
 
+// Population i of node (x, y) after the pull and the boundary rules, one population at a time
+// (for kernels that consume populations as they arrive instead of holding all Q).
+template <class L, class S, class CT>
+__device__ __forceinline__ typename S::C pop_streamed(const StepParams<CT>& p, const typename S::T* __restrict__ src,
+                                                      int x, int y, const int* xw, const int* yo, bool near, int i) {
+  typename S::C v = S::ld(src + (size_t)i * p.n + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
+  if (near) {
+    const int node = y * p.nx + x;
+    const int y1 = y + 1, x1 = x + 1;
+    const int o = L::opp(i);
+    for (int b = 0; b < p.nbc; ++b) {
+      const BCDev& bc = p.bc[b];
+      if (bc.kind == LBM_BOUNCE_BACK) {
+        if (x < bc.x_lo || x > bc.x_hi || y < bc.y_lo || y > bc.y_hi) continue;
+        bool hit;
+        if (bc.dir == LBM_NORTH) hit = y1 + L::cy(o) > p.ny;
+        else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
+        else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
+        else hit = x1 + L::cx(o) <= 0;
+        if (hit) v = S::ld(src + (size_t)o * p.n + node);
+      } else if (y1 + L::cy(o) > p.ny) {
+        v = S::ld(src + (size_t)o * p.n + node) + (typename S::C)bc.add[i];
+      }
+    }
+  }
+  return v;
+}
+
 template <class L, class S, class CT>
 __device__ __forceinline__ void load_local(const StepParams<CT>& p, const typename S::T* __restrict__ src,
                                            int node, typename S::C* f) {
@@ -159,22 +187,69 @@ __host__ __device__ constexpr int mom_count(int hn) { return hn <= 1 ? 3 : hn ==
 // DEV: v holds g = f - w and receives g_out = f_out - w.  The weights' own Hermite moments
 // of orders 1..N vanish (the quadrature symmetry the reference tests, test/quadrature.jl:1-19),
 // so the coefficients of f equal those formed from g, with ρ - 1 in place of ρ where M_00 enters.
-template <class L, bool DEV, class CT>
-__device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
+template <class CT>
+struct MrtCoeffs {
+  CT B[15];      // coefficients of the monomials c_x^a c_y^b of f_out / w
+  CT B1p, B2p;   // deviation storage: first-order coefficients per w1 = c w
+};
+
+template <class L, class CT>
+__device__ __forceinline__ void mrt_accumulate(CT* M, int i, CT v) {
   constexpr int NM = mom_count(L::HN);
-  CT M[15];
 #pragma unroll
   for (int k = 0; k < NM; ++k) {
-    CT s = 0;
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
-      const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
-      if (coef == 1) s += v[i];
-      else if (coef == -1) s -= v[i];
-      else if (coef != 0) s += (CT)coef * v[i];
-    }
-    M[k] = s;
+    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
+    if (coef == 1) M[k] += v;
+    else if (coef == -1) M[k] -= v;
+    else if (coef != 0) M[k] += (CT)coef * v;
   }
+}
+
+// Pair form of mrt_accumulate: opposite populations i, opp(i) enter through s = f_i + f_opp and
+// d = f_i - f_opp, since c_opp = -c_i makes each monomial of odd degree flip sign.
+template <class L, class CT>
+__device__ __forceinline__ void mrt_accumulate_pair(CT* M, int i, CT s, CT d) {
+  constexpr int NM = mom_count(L::HN);
+#pragma unroll
+  for (int k = 0; k < NM; ++k) {
+    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
+    const CT v = ((mom_a(k) + mom_b(k)) & 1) ? d : s;
+    if (coef == 1) M[k] += v;
+    else if (coef == -1) M[k] -= v;
+    else if (coef != 0) M[k] += (CT)coef * v;
+  }
+}
+
+// Pair form of mrt_out: the even- and odd-degree parts E, O of population i give
+// f_i = w (E + O) and f_opp = w (E - O).
+template <class L, bool DEV, class CT>
+__device__ __forceinline__ void mrt_out_pair(const StepParams<CT>& p, const MrtCoeffs<CT>& c, int i, CT& out_i,
+                                             CT& out_o) {
+  constexpr int NM = mom_count(L::HN);
+  CT E = c.B[0], O = 0;
+#pragma unroll
+  for (int k = DEV ? 3 : 1; k < NM; ++k) {
+    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
+    CT& acc = ((mom_a(k) + mom_b(k)) & 1) ? O : E;
+    if (coef == 1) acc += c.B[k];
+    else if (coef == -1) acc -= c.B[k];
+    else if (coef != 0) acc += (CT)coef * c.B[k];
+  }
+  CT we = p.w[i] * E, wo = p.w[i] * O;
+  if constexpr (DEV) {
+    CT s1 = 0;
+    if (L::cx(i) != 0) s1 += (CT)L::cx(i) * c.B1p;
+    if (L::cy(i) != 0) s1 += (CT)L::cy(i) * c.B2p;
+    wo += p.w1[i] * s1;
+  }
+  out_i = we + wo;
+  out_o = we - wo;
+}
+
+// Relaxation of the Hermite coefficients from the raw moments M (see mrt_collide).
+template <class L, bool DEV, class CT>
+__device__ __forceinline__ void mrt_coeffs(const StepParams<CT>& p, const CT* M, CT Fx, CT Fy, bool has_force,
+                                           MrtCoeffs<CT>& c) {
   const CT rho = DEV ? (CT)1 + M[0] : M[0];
   const CT inv_rho = (CT)1 / rho;
   CT ux = M[1] * inv_rho, uy = M[2] * inv_rho;
@@ -183,13 +258,14 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
     uy += p.shift * Fy;
   }
   const CT cs = p.cs, ics = (CT)1 / cs;  // ics = c_s^2
-  CT B[15];
+  CT* B = c.B;
 #pragma unroll
   for (int k = 0; k < 15; ++k) B[k] = 0;
   B[0] = M[0];  // ρ, or ρ - 1 in deviation form
   B[1] = cs * rho * ux;
   B[2] = cs * rho * uy;
-  CT B1p = rho * ux, B2p = rho * uy;  // deviation storage: first-order coefficients per w1 = cs w
+  c.B1p = rho * ux;
+  c.B2p = rho * uy;
   if constexpr (L::HN >= 2) {
     const CT a = p.mrt_a[1], b = p.mrt_b[1];
     const CT Axx = a * (M[3] - ics * M[0]) + b * (rho * ux * ux);
@@ -214,8 +290,8 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
     B[9] += c3 * Ayyy;
     B[1] -= c3 * (CT)3 * ics * (Axxx + Axyy);
     B[2] -= c3 * (CT)3 * ics * (Axxy + Ayyy);
-    B1p -= c3 * (CT)3 * ics * ics * (Axxx + Axyy);
-    B2p -= c3 * (CT)3 * ics * ics * (Axxy + Ayyy);
+    c.B1p -= c3 * (CT)3 * ics * ics * (Axxx + Axyy);
+    c.B2p -= c3 * (CT)3 * ics * ics * (Axxy + Ayyy);
   }
   if constexpr (L::HN >= 4) {
     const CT a = p.mrt_a[3], b = p.mrt_b[3];
@@ -236,40 +312,63 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
     B[5] -= c4 * ics * (CT)6 * (Axxyy + Ayyyy);
     B[0] += c4 * ics2 * ((CT)3 * Axxxx + (CT)6 * Axxyy + (CT)3 * Ayyyy);
   }
-  // Deviation storage: the first-order monomials carry w1_i / cs instead of w_i (see collide_node)
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) {
-    CT s = B[0];
-#pragma unroll
-    for (int k = DEV ? 3 : 1; k < NM; ++k) {
-      const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
-      if (coef == 1) s += B[k];
-      else if (coef == -1) s -= B[k];
-      else if (coef != 0) s += (CT)coef * B[k];
-    }
-    if constexpr (DEV) {
-      CT s1 = 0;
-      if (L::cx(i) != 0) s1 += (CT)L::cx(i) * B1p;
-      if (L::cy(i) != 0) s1 += (CT)L::cy(i) * B2p;
-      v[i] = p.w[i] * s + p.w1[i] * s1;
-    } else {
-      v[i] = p.w[i] * s;
-    }
-  }
-  (void)B1p;
-  (void)B2p;
 }
 
-// SRT / TRT in deviation storage for velocity sets whose equilibrium is of order <= 2 (D2Q4,
-// D2Q5, D2Q9, D2Q13), in "pair form".  Opposite populations enter only through their sum s and
-// difference d, which give both the moments (δρ = Σ s, j = Σ c d) and the TRT symmetric /
-// antisymmetric parts; the equilibrium is built from j' = ρ(u + τF) directly:
+// Post-collision population i rebuilt from the coefficients.  Deviation storage: the first-order
+// monomials carry w1_i / c instead of w_i (see collide_pairs).
+template <class L, bool DEV, class CT>
+__device__ __forceinline__ CT mrt_out(const StepParams<CT>& p, const MrtCoeffs<CT>& c, int i) {
+  constexpr int NM = mom_count(L::HN);
+  CT s = c.B[0];
+#pragma unroll
+  for (int k = DEV ? 3 : 1; k < NM; ++k) {
+    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
+    if (coef == 1) s += c.B[k];
+    else if (coef == -1) s -= c.B[k];
+    else if (coef != 0) s += (CT)coef * c.B[k];
+  }
+  if constexpr (DEV) {
+    CT s1 = 0;
+    if (L::cx(i) != 0) s1 += (CT)L::cx(i) * c.B1p;
+    if (L::cy(i) != 0) s1 += (CT)L::cy(i) * c.B2p;
+    return p.w[i] * s + p.w1[i] * s1;
+  } else {
+    return p.w[i] * s;
+  }
+}
+
+// Regularised MRT collision on one node (mrt.jl:135-197), written with raw moments: the
+// Hermite coefficients a_f^(n) = Σ f_i H_n(c_i) of orders 2..N are formed from the raw
+// moments M_ab, relaxed towards a_eq^(n) = ρ u^{⊗n}, and the populations are rebuilt as
+// w_i (ρ + cs ρ u·c_i + Σ_n cs^n / n! a_coll^(n) : H_n(c_i)), expanded in monomials of c_i.
+// DEV: v holds g = f - w and receives g_out = f_out - w.  The weights' own Hermite moments
+// of orders 1..N vanish (the quadrature symmetry the reference tests, test/quadrature.jl:1-19),
+// so the coefficients of f equal those formed from g, with ρ - 1 in place of ρ where M_00 enters.
+template <class L, bool DEV, class CT>
+__device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
+  CT M[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) M[k] = 0;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) mrt_accumulate<L>(M, i, v[i]);
+  MrtCoeffs<CT> c;
+  mrt_coeffs<L, DEV>(p, M, Fx, Fy, has_force, c);
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) v[i] = mrt_out<L, DEV>(p, c, i);
+}
+
+// SRT / TRT in "pair form" (all storages).  Opposite populations enter only through their
+// sum s and difference d, which give both the moments (δρ = Σ s, j = Σ c d) and the TRT
+// symmetric / antisymmetric parts; the equilibrium is built from j' = ρ(u + τF) directly, with
+// X = c_i·j', J² = |j'|², c = 1/c_s²:
 //   feq_i = S + A,  feq_opp(i) = S - A,
-//   S = w δρ + w ((c²/2)(c_i·j')² - (c/2)|j'|²) / ρ,   A = w1 (c_i·j'),   c = 1/c_s²,
-// and the update is f'_i = Ys + Ya, f'_opp = Ys - Ya with Ys = (1 - ω_s) s/2 + ω_s S,
-// Ya = (1 - ω_a) d/2 + ω_a A (srt.jl:18-62 and trt.jl:42-97 rewritten; SRT is ω_s = ω_a).
-template <class L, class CT>
-__device__ __forceinline__ void collide_pairs_dev(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
+//   S = w δρ + w (c²X² - cJ²) / (2ρ) [+ w (c⁴X⁴ - 6c³J²X² + 3c²J⁴) / (24ρ³)  fourth order]
+//   A = w1 X                          [+ w c X (c²X² - 3cJ²) / (6ρ²)          third order]
+// (the truncations of velocity_distribution_function/*.jl written in j'), and the update is
+// f'_i = Ys + Ya, f'_opp = Ys - Ya with Ys = (1 - ω_s) s/2 + ω_s S, Ya = (1 - ω_a) d/2 + ω_a A
+// (srt.jl:18-62 and trt.jl:42-97 rewritten; SRT is ω_s = ω_a).
+template <class L, bool DEV, class CT>
+__device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
   CT sp[L::Q], dp[L::Q];
   CT drho = 0;
 #pragma unroll
@@ -295,21 +394,36 @@ __device__ __forceinline__ void collide_pairs_dev(const StepParams<CT>& p, CT* v
     else if (L::cy(i) == -1) jy -= dp[i];
     else if (L::cy(i) != 0) jy += (CT)L::cy(i) * dp[i];
   }
-  const CT rho = (CT)1 + drho;
+  // FP64 storage holds f, so `drho` is ρ itself and w·drho below is w ρ; deviation storage
+  // holds g = f - w, so it is ρ - 1 and w·drho is the deviation w (ρ - 1) of the rest state
+  const CT rho = DEV ? (CT)1 + drho : drho;
   const CT inv = (CT)1 / rho;
   if (has_force) {  // j' = ρ (u + τ F)
     const CT rs = rho * p.shift;
     jx += rs * Fx;
     jy += rs * Fy;
   }
-  CT q2 = 0;
-  if constexpr (L::EQ >= 2) q2 = (p.hcs * (jx * jx + jy * jy)) * inv;
+  CT q2 = 0, J2 = 0, inv2 = 0, c3 = 0, c4 = 0, q4 = 0, cs3J2 = 0;
+  if constexpr (L::EQ >= 2) {
+    J2 = jx * jx + jy * jy;
+    q2 = (p.hcs * J2) * inv;
+  }
+  if constexpr (L::EQ >= 3) {
+    inv2 = inv * inv;
+    c3 = p.cs * (CT)(1.0 / 6.0) * inv2;  // c / (6 ρ²)
+    cs3J2 = (CT)3 * p.cs * J2;           // 3 c J²
+  }
+  if constexpr (L::EQ >= 4) {
+    c4 = (CT)(1.0 / 24.0) * inv2 * inv;  // 1 / (24 ρ³)
+    q4 = (CT)3 * (p.cs * p.cs) * (J2 * J2);
+  }
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) {
     const int o = L::opp(i);
     if (o == i) {
       CT S = p.w[i] * drho;
       if constexpr (L::EQ >= 2) S -= p.w[i] * q2;
+      if constexpr (L::EQ >= 4) S += p.w[i] * (q4 * c4);
       v[i] = ((CT)2 * p.pa_s) * v[i] + p.pom_s * S;
     } else if (o > i) {
       CT X = 0;
@@ -320,8 +434,14 @@ __device__ __forceinline__ void collide_pairs_dev(const StepParams<CT>& p, CT* v
       else if (L::cy(i) == -1) X -= jy;
       else if (L::cy(i) != 0) X += (CT)L::cy(i) * jy;
       CT S = p.w[i] * drho;
-      if constexpr (L::EQ >= 2) S += p.w[i] * ((p.hcs2 * (X * X)) * inv - q2);
-      const CT A = p.w1[i] * X;
+      const CT X2 = X * X;
+      if constexpr (L::EQ >= 2) S += p.w[i] * ((p.hcs2 * X2) * inv - q2);
+      if constexpr (L::EQ >= 4) {
+        const CT cs2 = p.cs * p.cs;
+        S += p.w[i] * (((cs2 * cs2) * (X2 * X2) - ((CT)6 * (cs2 * p.cs)) * (J2 * X2) + q4) * c4);
+      }
+      CT A = p.w1[i] * X;
+      if constexpr (L::EQ >= 3) A += p.w[i] * ((X * ((p.cs * p.cs) * X2 - cs3J2)) * c3);
       const CT Ys = p.pa_s * sp[i] + p.pom_s * S;
       const CT Ya = p.pa_a * dp[i] + p.pom_a * A;
       v[i] = Ys + Ya;
@@ -344,8 +464,8 @@ __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int
   if constexpr (COLL == LBM_MRT) {
     mrt_collide<L, DEV>(p, v, Fx, Fy, has_force);
     return;
-  } else if constexpr (DEV && L::EQ <= 2 && (COLL == LBM_SRT || COLL == LBM_TRT)) {
-    collide_pairs_dev<L>(p, v, Fx, Fy, has_force);
+  } else if constexpr (COLL == LBM_SRT || COLL == LBM_TRT) {
+    collide_pairs<L, DEV>(p, v, Fx, Fy, has_force);
     return;
   } else {
     CT s = v[0];
@@ -439,12 +559,57 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
   if (x >= p.nx) return;
   for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
     const int node = y * p.nx + x;
-    CT v[L::Q];
-    if (MODE == 0) load_local<L, S>(p, src, node, v);
-    else load_streamed<L, S>(p, src, x, y, v);
-    if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v);
+    if constexpr (COLL == LBM_MRT && MODE != 2) {
+      // streaming form: populations feed the raw moments as they arrive, outputs are rebuilt
+      // and stored one by one, so no per-node array of Q populations stays live
+      CT M[15];
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) S::st(dst + (size_t)i * p.n + node, v[i]);
+      for (int k = 0; k < 15; ++k) M[k] = 0;
+      int xw[2 * L::R + 1], yo[2 * L::R + 1];
+      bool near = false;
+      if (MODE != 0) {
+        pull_offsets<L>(p, x, y, xw, yo);
+        near = p.nbc > 0 && (y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R);
+      }
+      auto pop = [&](int i) -> CT {
+        if (MODE == 0) return S::ld(src + (size_t)i * p.n + node);
+        return pop_streamed<L, S>(p, src, x, y, xw, yo, near, i);
+      };
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const int o = L::opp(i);
+        if (o == i) {
+          M[0] += pop(i);
+        } else if (o > i) {
+          const CT a = pop(i), b = pop(o);
+          mrt_accumulate_pair<L>(M, i, a + b, a - b);
+        }
+      }
+      CT Fx = 0, Fy = 0;
+      const bool has_force = p.force_kind != LBM_FORCE_NONE;
+      if (has_force) node_force(p, x, y, Fx, Fy);
+      MrtCoeffs<CT> c;
+      mrt_coeffs<L, S::DEV>(p, M, Fx, Fy, has_force, c);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const int o = L::opp(i);
+        if (o == i) {
+          S::st(dst + (size_t)i * p.n + node, p.w[i] * c.B[0]);
+        } else if (o > i) {
+          CT a, b;
+          mrt_out_pair<L, S::DEV>(p, c, i, a, b);
+          S::st(dst + (size_t)i * p.n + node, a);
+          S::st(dst + (size_t)o * p.n + node, b);
+        }
+      }
+    } else {
+      CT v[L::Q];
+      if (MODE == 0) load_local<L, S>(p, src, node, v);
+      else load_streamed<L, S>(p, src, x, y, v);
+      if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) S::st(dst + (size_t)i * p.n + node, v[i]);
+    }
   }
 }
 

@@ -202,3 +202,51 @@ class DeviceLattice:
 
     def apply_bcs_device(self, f_new, f_old):
         N.check(self.h, N.lib().lbm_apply_bcs_device(self.h, N.ptr(f_new), N.ptr(f_old)))
+
+
+class DeviceBatch:
+    """Several DeviceLattices advanced together: member k takes nsteps[k] steps, all issued as one
+    CUDA graph with one kernel per global step over every member still running (lbm_batch_*).
+    Members must share storage and collision kind (SRT / TRT), use D2Q4..D2Q17 and no
+    time-dependent force."""
+
+    def __init__(self, lattices):
+        L = N.lib()
+        self.lattices = list(lattices)
+        arr = (C.c_void_p * len(self.lattices))(*[lat.h.value for lat in self.lattices])
+        h = C.c_void_p()
+        st = L.lbm_batch_create(C.byref(h), arr, len(self.lattices))
+        if st != N.LBM_OK:
+            raise N.LbmError(st, "lbm_batch_create: members must share storage and SRT/TRT collision, "
+                                 "use D2Q4..D2Q17 and no time-dependent force")
+        self.h = h
+
+    def _check(self, st):
+        if st != N.LBM_OK:
+            raise N.LbmError(st, N.lib().lbm_batch_last_error(self.h).decode())
+
+    def step(self, nsteps):
+        ns = np.ascontiguousarray(nsteps, dtype=np.int64)
+        if ns.shape != (len(self.lattices),):
+            raise ValueError("one step count per member")
+        self._check(N.lib().lbm_batch_step(self.h, ns.ctypes.data_as(C.POINTER(C.c_int64))))
+
+    def set_stream(self, stream_handle):
+        self._check(N.lib().lbm_batch_set_stream(self.h, stream_handle or None))
+
+    def synchronize(self):
+        self._check(N.lib().lbm_batch_synchronize(self.h))
+
+    def last_launch_count(self) -> int:
+        return int(N.lib().lbm_batch_last_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().lbm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,118 @@
+"""Adjoint gradients (lbm_adjoint_*) against central finite differences of the device forward
+model (FP64) and of the oracle's CPU restatement of the reference loop."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NX = NY = 32
+STEPS = 120
+
+
+def _setup(lbm, storage="f64", nsteps=STEPS, tau_s=0.8, F=(2e-6, -1e-6), ck=0):
+    q = lbm.D2Q9()
+    tau_a = lbm.trt_magic(tau_s)
+    return lbm.AdjointProblem(q, NX, NY, lbm.TRT.fields(tau_s, tau_a), force=F, nsteps=nsteps,
+                              checkpoint_every=ck, storage=storage)
+
+
+def _fields(lbm):
+    u0 = lbm.divergence_free_field(NX, NY, kmax=4, amplitude=0.01, seed=1)
+    ut = lbm.divergence_free_field(NX, NY, kmax=4, amplitude=0.01, seed=2)
+    return u0, ut
+
+
+def _loss(lbm, u0, ut, tau_s, tau_a, F, storage="f64"):
+    q = lbm.D2Q9()
+    p = lbm.AdjointProblem(q, NX, NY, lbm.TRT.fields(tau_s, tau_a), force=F, nsteps=STEPS, storage=storage)
+    L = p.loss(u0, ut)
+    p.close()
+    return L
+
+
+def test_adjoint_matches_finite_differences(lbm_gpu):
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    tau_s, F = 0.8, (2e-6, -1e-6)
+    tau_a = lbm.trt_magic(tau_s)
+    prob = _setup(lbm, tau_s=tau_s, F=F)
+    res = prob.run(u0, ut)
+    prob.close()
+    h = 1e-6
+    fd_ts = (_loss(lbm, u0, ut, tau_s + h, tau_a, F) - _loss(lbm, u0, ut, tau_s - h, tau_a, F)) / (2 * h)
+    fd_ta = (_loss(lbm, u0, ut, tau_s, tau_a + h, F) - _loss(lbm, u0, ut, tau_s, tau_a - h, F)) / (2 * h)
+    hF = 1e-7
+    fd_fx = (_loss(lbm, u0, ut, tau_s, tau_a, (F[0] + hF, F[1])) -
+             _loss(lbm, u0, ut, tau_s, tau_a, (F[0] - hF, F[1]))) / (2 * hF)
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=u0.shape)
+    hu = 1e-6
+    fd_u = (_loss(lbm, u0 + hu * v, ut, tau_s, tau_a, F) - _loss(lbm, u0 - hu * v, ut, tau_s, tau_a, F)) / (2 * hu)
+    for ad, fd in [(res["dtau_s"], fd_ts), (res["dtau_a"], fd_ta), (res["dF"][0], fd_fx),
+                   (float(np.sum(res["grad_u0"] * v)), fd_u)]:
+        assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-12), (ad, fd)
+
+
+def test_adjoint_matches_oracle_finite_differences(lbm_gpu, O):
+    """The same loss evaluated with the oracle's collide -> stream loop (the CPU restatement of
+    the reference) gives the same value and central differences as the adjoint."""
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    tau_s, F = 0.8, (2e-6, -1e-6)
+    tau_a = lbm.trt_magic(tau_s)
+
+    def oracle_loss(ts, ta, u):
+        p = O.poiseuille_struct(1.0, 0.05, 0.1, NX, NY, 1.0, (1.0, 1.0), 1.0)
+        sc = O.problem_scalars(p)
+        p.G = F[0] / (p.u_max * sc["delta_t"] * sc["viscosity"])
+        f0 = np.empty((9, NY, NX))
+        for y in range(NY):
+            for x in range(NX):
+                f0[:, y, x] = O.equilibrium("D2Q9", 1.0, (u[0, y, x], u[1, y, x]))
+        f = O.run("D2Q9", p, O.collision("TRT", [ts, ta], force=True), [], f0, 0, STEPS - 1, dt=sc["delta_t"])
+        rho = f.sum(axis=0)
+        cx = np.array([0, -1, -1, -1, 0, 1, 1, 1, 0])
+        cy = np.array([0, 1, 0, -1, -1, -1, 0, 1, 1])
+        ux = np.tensordot(cx, f, 1) / rho
+        uy = np.tensordot(cy, f, 1) / rho
+        return float(np.sum((ux - ut[0]) ** 2 + (uy - ut[1]) ** 2))
+
+    Fx_only = (F[0], 0.0)  # the oracle's Poiseuille force is along x
+    prob = _setup(lbm, tau_s=tau_s, F=Fx_only)
+    res = prob.run(u0, ut)
+    prob.close()
+    assert res["loss"] == pytest.approx(oracle_loss(tau_s, tau_a, u0), rel=1e-10)
+    h = 1e-6
+    fd_ts = (oracle_loss(tau_s + h, tau_a, u0) - oracle_loss(tau_s - h, tau_a, u0)) / (2 * h)
+    assert abs(res["dtau_s"] - fd_ts) <= 1e-6 * abs(fd_ts)
+    rng = np.random.default_rng(3)
+    v = rng.normal(size=u0.shape)
+    fd_u = (oracle_loss(tau_s, tau_a, u0 + h * v) - oracle_loss(tau_s, tau_a, u0 - h * v)) / (2 * h)
+    assert abs(float(np.sum(res["grad_u0"] * v)) - fd_u) <= 1e-6 * abs(fd_u)
+
+
+def test_checkpoint_interval_does_not_change_gradients(lbm_gpu):
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    outs = []
+    for ck in (1, 7, 0, STEPS):
+        prob = _setup(lbm, ck=ck)
+        outs.append(prob.run(u0, ut))
+        prob.close()
+    for o in outs[1:]:
+        assert o["loss"] == outs[0]["loss"]
+        np.testing.assert_array_equal(o["grad_u0"], outs[0]["grad_u0"])
+        assert o["dtau_s"] == outs[0]["dtau_s"]
+
+
+def test_fp32_adjoint_close_to_fp64(lbm_gpu):
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    r = {}
+    for st in ("f64", "f32dev"):
+        prob = _setup(lbm, storage=st)
+        r[st] = prob.run(u0, ut)
+        prob.close()
+    assert r["f32dev"]["loss"] == pytest.approx(r["f64"]["loss"], rel=1e-4)
+    g64, g32 = r["f64"]["grad_u0"], r["f32dev"]["grad_u0"]
+    assert np.max(np.abs(g32 - g64)) <= 1e-3 * np.max(np.abs(g64))
