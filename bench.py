@@ -309,6 +309,9 @@ def main():
     ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev"])
     ap.add_argument("--profile", action="store_true",
                     help="time only the device loop of the chosen storage (for profiler runs)")
+    ap.add_argument("--case", default="poiseuille", choices=["poiseuille", "mrt_d2q37"],
+                    help="with --profile: the lattice whose device loop is timed (D2Q9 TRT Poiseuille "
+                         "4096^2, or D2Q37 regularised MRT shear wave 2048^2)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other configurations (Taylor-Green 64^2, D2Q37 MRT, batched study, adjoint)")
     args = ap.parse_args()
@@ -327,6 +330,18 @@ def main():
     lbm = __graft_entry__.load_package()
     lbm._native.lib()
     tau_s = tau_from_seed()
+
+    if args.profile and args.case == "mrt_d2q37":
+        q = lbm.D2Q37()
+        n = 2048
+        problem = lbm.ShearWave(n, n, (0.6 - 0.5) / q.speed_of_sound_squared, 0.01)
+        f0 = lbm.initialize(lbm.AnalyticalEquilibrium(), q, problem)
+        m = lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.MRT(q, 0.6), storage=args.storage, f0=f0)
+        sec, launches = time_device(torch, m, args.steps, args.warmup, 1.0)
+        m.close()
+        print(json.dumps({"case": "mrt_d2q37", "storage": args.storage, "mlups": n * n * args.steps / sec / 1e6,
+                          "launches": launches}))
+        return 0
 
     problem, model, f0 = build_model(lbm, args.storage, tau_s)
     dt = problem.delta_t()

@@ -299,6 +299,19 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
     }
   }
 
+  // The pair forms give both members of a velocity class {(±a, ±b), (±b, ±a)} one weight (the
+  // quadratures of the reference all have this symmetry); other weight tables are rejected.
+  for (int i = 0; i < c->Q; ++i)
+    for (int j = 0; j < c->Q; ++j) {
+      const int ai = std::abs(c->lat.cx[i]), bi = std::abs(c->lat.cy[i]);
+      const int aj = std::abs(c->lat.cx[j]), bj = std::abs(c->lat.cy[j]);
+      if (std::min(ai, bi) == std::min(aj, bj) && std::max(ai, bi) == std::max(aj, bj) &&
+          d->weights[i] != d->weights[j]) {
+        delete c;
+        return LBM_ERR_INVALID;
+      }
+    }
+
   // parameter blocks (FP64 and FP32 copies; the storage selects one)
   StepParams<double>& p = c->pd;
   p.nx = (int)d->nx;
@@ -337,9 +350,14 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   }
   p.hcs = p.cs / 2;
   p.hcs2 = p.cs * p.cs / 2;
+  for (int i = 0; i < LBM_MAX_Q; ++i) p.pws[i] = p.pom_s * p.w[i];
+  for (int i = 0; i < LBM_MAX_Q; ++i) p.pwa[i] = p.pom_a * p.w[i];
+  p.pa_s2 = 2 * p.pa_s;
   p.force_kind = d->force_kind;
   p.F[0] = d->force[0];
   p.F[1] = d->force[1];
+  p.sF[0] = p.shift * p.F[0];
+  p.sF[1] = p.shift * p.F[1];
   for (int k = 0; k < 6; ++k) p.shear[k] = d->shear[k];
   p.nbc = d->nbc;
   for (int b = 0; b < d->nbc; ++b) {
@@ -384,6 +402,11 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   q.pom_a = (float)p.pom_a;
   q.hcs = (float)p.hcs;
   q.hcs2 = (float)p.hcs2;
+  for (int i = 0; i < LBM_MAX_Q; ++i) q.pws[i] = (float)p.pws[i];
+  for (int i = 0; i < LBM_MAX_Q; ++i) q.pwa[i] = (float)p.pwa[i];
+  q.pa_s2 = (float)p.pa_s2;
+  q.sF[0] = (float)p.sF[0];
+  q.sF[1] = (float)p.sF[1];
   for (int k = 0; k < 4; ++k) {
     q.mrt_a[k] = (float)p.mrt_a[k];
     q.mrt_b[k] = (float)p.mrt_b[k];
@@ -402,6 +425,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   // representable exactly is preferred (D2Q4/5/9/13: exact; D2Q17/37: residual ~1e-10).
   {
     for (int i = 0; i < LBM_MAX_Q; ++i) p.w1[i] = i < c->Q ? p.cs * p.w[i] : 0.0;
+    for (int i = 0; i < LBM_MAX_Q; ++i) p.pw1a[i] = p.pom_a * p.w1[i];
     float w1f[LBM_MAX_Q];
     for (int i = 0; i < LBM_MAX_Q; ++i) w1f[i] = (float)p.w1[i];
     long double best_res = -1.0L;
@@ -436,6 +460,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
       }
     }
     for (int i = 0; i < LBM_MAX_Q; ++i) q.w1[i] = w1f[i];
+    for (int i = 0; i < LBM_MAX_Q; ++i) q.pw1a[i] = (float)p.pom_a * w1f[i];
   }
   // float-float copy (every constant split once on the host)
   StepParams<dd>& x = c->px;
@@ -460,6 +485,12 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   x.pom_a = dd(p.pom_a);
   x.hcs = dd(p.hcs);
   x.hcs2 = dd(p.hcs2);
+  for (int i = 0; i < LBM_MAX_Q; ++i) x.pws[i] = dd(p.pws[i]);
+  for (int i = 0; i < LBM_MAX_Q; ++i) x.pwa[i] = dd(p.pwa[i]);
+  for (int i = 0; i < LBM_MAX_Q; ++i) x.pw1a[i] = dd(p.pom_a * p.w1[i]);
+  x.pa_s2 = dd(p.pa_s2);
+  x.sF[0] = dd(p.sF[0]);
+  x.sF[1] = dd(p.sF[1]);
   for (int k = 0; k < 4; ++k) {
     x.mrt_a[k] = dd(p.mrt_a[k]);
     x.mrt_b[k] = dd(p.mrt_b[k]);

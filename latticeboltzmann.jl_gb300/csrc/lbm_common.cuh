@@ -7,10 +7,39 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "../../include/lbm_gb300.h"
 #include "lbm_df64.cuh"
 
 namespace lbm {
+
+// Compile-time loop: calls f(std::integral_constant<int, k>) for k = B .. E-1, so velocity and
+// moment indices are constants inside the body and every lattice-table lookup, power and
+// coefficient of the velocity set folds away.
+template <int B, int E, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    static_for<B + 1, E>(f);
+  }
+}
+
+// v (+)= C t for a compile-time integer C; the first term initialises v, since IEEE arithmetic
+// cannot fold a leading 0 + t away.  `set` is a constant at every point of an unrolled loop.
+template <int C, class CT>
+__device__ __forceinline__ void acc_add(CT& v, bool& set, CT t) {
+  if constexpr (C == 1) {
+    v = set ? v + t : t;
+    set = true;
+  } else if constexpr (C == -1) {
+    v = set ? v - t : -t;
+    set = true;
+  } else if constexpr (C != 0) {
+    v = set ? v + (CT)C * t : (CT)C * t;
+    set = true;
+  }
+}
 
 // ---------------------------------------------------------------------------------------
 // Velocity sets.  Abscissae and opposite maps as in src/quadratures/D2Q*.jl and
@@ -123,6 +152,11 @@ struct StepParams {
   CT shift;                    // force velocity shift: τ (SRT), τ_a (TRT), τs[2] (MRT)
   CT pa_s, pa_a, pom_s, pom_a; // pair form: (1 - ω_s)/2, (1 - ω_a)/2, ω_s, ω_a (SRT: ω_s = ω_a = 1/τ)
   CT hcs, hcs2;                // pair form: (1/c_s²)/2, (1/c_s²)²/2
+  CT pws[LBM_MAX_Q];           // pair form: ω_s w_i
+  CT pwa[LBM_MAX_Q];           // pair form: ω_a w_i
+  CT pw1a[LBM_MAX_Q];          // pair form: ω_a w1_i
+  CT pa_s2;                    // pair form: 1 - ω_s (rest population)
+  CT sF[2];                    // CONSTANT force times the velocity shift
   CT w1[LBM_MAX_Q];            // deviation storage: first-order equilibrium coefficients (1/c_s²)·w_i,
                                // chosen so that Σ_i w1_i c_ix² = 1 holds for the values as stored
   CT mrt_a[4], mrt_b[4];       // MRT: (1 - 1/τ_n), 1/τ_n for n = 1..4

@@ -135,6 +135,20 @@ __device__ __forceinline__ void node_force(const StepParams<CT>& p, int x, int y
     Fy = 0;
   }
 }
+// Lattice force at node (x, y) times the velocity shift (τ for SRT, τ_a for TRT, τ_2 for MRT),
+// i.e. the term the collision adds to u; for a CONSTANT force the product comes from the host.
+template <class CT>
+__device__ __forceinline__ void node_shifted_force(const StepParams<CT>& p, int x, int y, CT& sFx, CT& sFy) {
+  if (p.force_kind == LBM_FORCE_CONSTANT) {
+    sFx = p.sF[0];
+    sFy = p.sF[1];
+  } else {
+    CT Fx, Fy;
+    node_force(p, x, y, Fx, Fy);
+    sFx = p.shift * Fx;
+    sFy = p.shift * Fy;
+  }
+}
 
 // `equilibrium!` truncation by velocity set: first order (D2Q4/5), second (D2Q9/13), third
 // (D2Q17/21), fourth (D2Q37).  Returns the bracket 1 + a1 + a2/2 [+ a3/6 + a4/24] minus 1,
@@ -180,82 +194,33 @@ __host__ __device__ constexpr int mom_b(int k) {
 __host__ __device__ constexpr int ipow(int c, int e) { return e == 0 ? 1 : c * ipow(c, e - 1); }
 __host__ __device__ constexpr int mom_count(int hn) { return hn <= 1 ? 3 : hn == 2 ? 6 : hn == 3 ? 10 : 15; }
 
-// Regularised MRT collision on one node (mrt.jl:135-197), written with raw moments: the
-// Hermite coefficients a_f^(n) = Σ f_i H_n(c_i) of orders 2..N are formed from the raw
-// moments M_ab, relaxed towards a_eq^(n) = ρ u^{⊗n}, and the populations are rebuilt as
-// w_i (ρ + cs ρ u·c_i + Σ_n cs^n / n! a_coll^(n) : H_n(c_i)), expanded in monomials of c_i.
-// DEV: v holds g = f - w and receives g_out = f_out - w.  The weights' own Hermite moments
-// of orders 1..N vanish (the quadrature symmetry the reference tests, test/quadrature.jl:1-19),
-// so the coefficients of f equal those formed from g, with ρ - 1 in place of ρ where M_00 enters.
 template <class CT>
 struct MrtCoeffs {
   CT B[15];      // coefficients of the monomials c_x^a c_y^b of f_out / w
   CT B1p, B2p;   // deviation storage: first-order coefficients per w1 = c w
 };
 
-template <class L, class CT>
-__device__ __forceinline__ void mrt_accumulate(CT* M, int i, CT v) {
-  constexpr int NM = mom_count(L::HN);
-#pragma unroll
-  for (int k = 0; k < NM; ++k) {
-    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
-    if (coef == 1) M[k] += v;
-    else if (coef == -1) M[k] -= v;
-    else if (coef != 0) M[k] += (CT)coef * v;
-  }
-}
-
-// Pair form of mrt_accumulate: opposite populations i, opp(i) enter through s = f_i + f_opp and
-// d = f_i - f_opp, since c_opp = -c_i makes each monomial of odd degree flip sign.
-template <class L, class CT>
-__device__ __forceinline__ void mrt_accumulate_pair(CT* M, int i, CT s, CT d) {
-  constexpr int NM = mom_count(L::HN);
-#pragma unroll
-  for (int k = 0; k < NM; ++k) {
-    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
-    const CT v = ((mom_a(k) + mom_b(k)) & 1) ? d : s;
-    if (coef == 1) M[k] += v;
-    else if (coef == -1) M[k] -= v;
-    else if (coef != 0) M[k] += (CT)coef * v;
-  }
-}
-
-// Pair form of mrt_out: the even- and odd-degree parts E, O of population i give
-// f_i = w (E + O) and f_opp = w (E - O).
-template <class L, bool DEV, class CT>
-__device__ __forceinline__ void mrt_out_pair(const StepParams<CT>& p, const MrtCoeffs<CT>& c, int i, CT& out_i,
-                                             CT& out_o) {
-  constexpr int NM = mom_count(L::HN);
-  CT E = c.B[0], O = 0;
-#pragma unroll
-  for (int k = DEV ? 3 : 1; k < NM; ++k) {
-    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
-    CT& acc = ((mom_a(k) + mom_b(k)) & 1) ? O : E;
-    if (coef == 1) acc += c.B[k];
-    else if (coef == -1) acc -= c.B[k];
-    else if (coef != 0) acc += (CT)coef * c.B[k];
-  }
-  CT we = p.w[i] * E, wo = p.w[i] * O;
-  if constexpr (DEV) {
-    CT s1 = 0;
-    if (L::cx(i) != 0) s1 += (CT)L::cx(i) * c.B1p;
-    if (L::cy(i) != 0) s1 += (CT)L::cy(i) * c.B2p;
-    wo += p.w1[i] * s1;
-  }
-  out_i = we + wo;
-  out_o = we - wo;
+// Raw moments accumulated pair by pair: opposite populations I, opp(I) enter through
+// s = f_I + f_opp and d = f_I - f_opp, since c_opp = -c_I flips every monomial of odd degree.
+template <class L, int I, class CT>
+__device__ __forceinline__ void mrt_accumulate_pair(CT* M, bool* set, CT s, CT d) {
+  static_for<0, mom_count(L::HN)>([&](auto K) {
+    constexpr int k = decltype(K)::value;
+    constexpr int coef = ipow(L::cx(I), mom_a(k)) * ipow(L::cy(I), mom_b(k));
+    acc_add<coef>(M[k], set[k], ((mom_a(k) + mom_b(k)) & 1) ? d : s);
+  });
 }
 
 // Relaxation of the Hermite coefficients from the raw moments M (see mrt_collide).
 template <class L, bool DEV, class CT>
-__device__ __forceinline__ void mrt_coeffs(const StepParams<CT>& p, const CT* M, CT Fx, CT Fy, bool has_force,
+__device__ __forceinline__ void mrt_coeffs(const StepParams<CT>& p, const CT* M, CT sFx, CT sFy, bool has_force,
                                            MrtCoeffs<CT>& c) {
   const CT rho = DEV ? (CT)1 + M[0] : M[0];
   const CT inv_rho = (CT)1 / rho;
   CT ux = M[1] * inv_rho, uy = M[2] * inv_rho;
   if (has_force) {
-    ux += p.shift * Fx;
-    uy += p.shift * Fy;
+    ux += sFx;
+    uy += sFy;
   }
   const CT cs = p.cs, ics = (CT)1 / cs;  // ics = c_s^2
   CT* B = c.B;
@@ -314,27 +279,30 @@ __device__ __forceinline__ void mrt_coeffs(const StepParams<CT>& p, const CT* M,
   }
 }
 
-// Post-collision population i rebuilt from the coefficients.  Deviation storage: the first-order
-// monomials carry w1_i / c instead of w_i (see collide_pairs).
-template <class L, bool DEV, class CT>
-__device__ __forceinline__ CT mrt_out(const StepParams<CT>& p, const MrtCoeffs<CT>& c, int i) {
-  constexpr int NM = mom_count(L::HN);
-  CT s = c.B[0];
-#pragma unroll
-  for (int k = DEV ? 3 : 1; k < NM; ++k) {
-    const int coef = ipow(L::cx(i), mom_a(k)) * ipow(L::cy(i), mom_b(k));
-    if (coef == 1) s += c.B[k];
-    else if (coef == -1) s -= c.B[k];
-    else if (coef != 0) s += (CT)coef * c.B[k];
-  }
+// Post-collision pair I, opp(I) rebuilt from the coefficients: the even- and odd-degree parts
+// E, O of population I give f_I = w (E + O) and f_opp = w (E - O).  Deviation storage: the
+// first-order monomials carry w1_I / c instead of w_I (see collide_pairs).
+template <class L, bool DEV, int I, class CT>
+__device__ __forceinline__ void mrt_out_pair(const StepParams<CT>& p, const MrtCoeffs<CT>& c, CT& out_i, CT& out_o) {
+  CT E = c.B[0], O;
+  bool se = true, so = false;
+  static_for<(DEV ? 3 : 1), mom_count(L::HN)>([&](auto K) {
+    constexpr int k = decltype(K)::value;
+    constexpr int coef = ipow(L::cx(I), mom_a(k)) * ipow(L::cy(I), mom_b(k));
+    if constexpr ((mom_a(k) + mom_b(k)) & 1) acc_add<coef>(O, so, c.B[k]);
+    else acc_add<coef>(E, se, c.B[k]);
+  });
+  const CT we = p.w[I] * E;
+  CT wo = so ? p.w[I] * O : (CT)0;
   if constexpr (DEV) {
-    CT s1 = 0;
-    if (L::cx(i) != 0) s1 += (CT)L::cx(i) * c.B1p;
-    if (L::cy(i) != 0) s1 += (CT)L::cy(i) * c.B2p;
-    return p.w[i] * s + p.w1[i] * s1;
-  } else {
-    return p.w[i] * s;
+    CT s1;
+    bool s1s = false;
+    acc_add<L::cx(I)>(s1, s1s, c.B1p);
+    acc_add<L::cy(I)>(s1, s1s, c.B2p);
+    wo = so ? wo + p.w1[I] * s1 : p.w1[I] * s1;
   }
+  out_i = we + wo;
+  out_o = we - wo;
 }
 
 // Regularised MRT collision on one node (mrt.jl:135-197), written with raw moments: the
@@ -344,17 +312,71 @@ __device__ __forceinline__ CT mrt_out(const StepParams<CT>& p, const MrtCoeffs<C
 // DEV: v holds g = f - w and receives g_out = f_out - w.  The weights' own Hermite moments
 // of orders 1..N vanish (the quadrature symmetry the reference tests, test/quadrature.jl:1-19),
 // so the coefficients of f equal those formed from g, with ρ - 1 in place of ρ where M_00 enters.
-template <class L, bool DEV, class CT>
-__device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
+// `pop(std::integral_constant<int, i>)` supplies population i; `out(i, value)` receives it.
+template <class L, bool DEV, class CT, class Pop, class Out>
+__device__ __forceinline__ void mrt_node(const StepParams<CT>& p, CT sFx, CT sFy, bool has_force, Pop&& pop,
+                                         Out&& out) {
+  constexpr int NM = mom_count(L::HN);
   CT M[15];
-#pragma unroll
-  for (int k = 0; k < 15; ++k) M[k] = 0;
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) mrt_accumulate<L>(M, i, v[i]);
+  bool ms[15];
+  static_for<0, 15>([&](auto K) { ms[decltype(K)::value] = false; });
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value, o = L::opp(i);
+    if constexpr (o == i) {
+      acc_add<1>(M[0], ms[0], pop(I));
+    } else if constexpr (o > i) {
+      const CT a = pop(I), b = pop(std::integral_constant<int, o>{});
+      mrt_accumulate_pair<L, i>(M, ms, a + b, a - b);
+    }
+  });
+  static_for<0, NM>([&](auto K) {
+    constexpr int k = decltype(K)::value;
+    if (!ms[k]) M[k] = (CT)0;
+  });
   MrtCoeffs<CT> c;
-  mrt_coeffs<L, DEV>(p, M, Fx, Fy, has_force, c);
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) v[i] = mrt_out<L, DEV>(p, c, i);
+  mrt_coeffs<L, DEV>(p, M, sFx, sFy, has_force, c);
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value, o = L::opp(i);
+    if constexpr (o == i) {
+      out(i, p.w[i] * c.B[0]);
+    } else if constexpr (o > i) {
+      CT a, b;
+      mrt_out_pair<L, DEV, i>(p, c, a, b);
+      out(i, a);
+      out(o, b);
+    }
+  });
+}
+
+template <class L, bool DEV, class CT>
+__device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT sFx, CT sFy, bool has_force) {
+  CT r[L::Q];
+  mrt_node<L, DEV>(p, sFx, sFy, has_force, [&](auto I) { return v[decltype(I)::value]; },
+                   [&](int i, CT val) { r[i] = val; });
+  static_for<0, L::Q>([&](auto I) { v[decltype(I)::value] = r[decltype(I)::value]; });
+}
+
+// 1/ρ for the O(u²) terms of the pair form.  FP64: a float reciprocal refined by one
+// Newton-Raphson step r (2 - ρ r), relative error ~1e-14, well below what the terms it scales
+// (u² ~ 1e-4 of f) need; FP32: the hardware reciprocal; float-float: recip() of lbm_df64.cuh.
+__device__ __forceinline__ double pair_recip(double r) {
+  const double r0 = (double)__frcp_rn((float)r);
+  return fma(r0, fma(-r, r0, 1.0), r0);
+}
+__device__ __forceinline__ float pair_recip(float r) { return __frcp_rn(r); }
+__device__ __forceinline__ dd pair_recip(dd r) { return recip(r); }
+
+// Velocity class of population i: the set {(±a, ±b), (±b, ±a)}, which shares one weight.
+template <class L>
+__host__ __device__ constexpr int vclass(int i) {
+  const int a = L::cx(i) < 0 ? -L::cx(i) : L::cx(i), b = L::cy(i) < 0 ? -L::cy(i) : L::cy(i);
+  return a < b ? a * 4 + b : b * 4 + a;
+}
+template <class L>
+__host__ __device__ constexpr bool class_first(int i) {
+  for (int j = 0; j < i; ++j)
+    if (vclass<L>(j) == vclass<L>(i)) return false;
+  return true;
 }
 
 // SRT / TRT in "pair form" (all storages).  Opposite populations enter only through their
@@ -366,88 +388,98 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT F
 //   A = w1 X                          [+ w c X (c²X² - 3cJ²) / (6ρ²)          third order]
 // (the truncations of velocity_distribution_function/*.jl written in j'), and the update is
 // f'_i = Ys + Ya, f'_opp = Ys - Ya with Ys = (1 - ω_s) s/2 + ω_s S, Ya = (1 - ω_a) d/2 + ω_a A
-// (srt.jl:18-62 and trt.jl:42-97 rewritten; SRT is ω_s = ω_a).
+// (srt.jl:18-62 and trt.jl:42-97 rewritten; SRT is ω_s = ω_a).  ω_s S and ω_a A are
+// polynomials in X whose coefficients depend on the node and the weight only, so they are
+// formed once per velocity class: ω_s S = b0 + X² (b2 + X² b4), ω_a A = X (ω_a w1 + a3 (c²X² - 3cJ²)).
+// FP32 keeps ω_a (w1 X) with the FP32-exact w1, so the equilibrium's momentum stays exact.
 template <class L, bool DEV, class CT>
-__device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT Fx, CT Fy, bool has_force) {
+__device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT sFx, CT sFy, bool has_force) {
+  constexpr bool F32 = std::is_same<CT, float>::value;
   CT sp[L::Q], dp[L::Q];
-  CT drho = 0;
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) {
-    const int o = L::opp(i);
-    if (o == i) {
-      drho += v[i];
-    } else if (o > i) {
+  CT drho, jx, jy;
+  bool sr = false, sx = false, sy = false;
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value, o = L::opp(i);
+    if constexpr (o == i) {
+      acc_add<1>(drho, sr, v[i]);
+    } else if constexpr (o > i) {
       sp[i] = v[i] + v[o];
       dp[i] = v[i] - v[o];
-      drho += sp[i];
+      acc_add<1>(drho, sr, sp[i]);
     }
-  }
-  CT jx = 0, jy = 0;
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) {
-    const int o = L::opp(i);
-    if (o <= i) continue;
-    if (L::cx(i) == 1) jx += dp[i];
-    else if (L::cx(i) == -1) jx -= dp[i];
-    else if (L::cx(i) != 0) jx += (CT)L::cx(i) * dp[i];
-    if (L::cy(i) == 1) jy += dp[i];
-    else if (L::cy(i) == -1) jy -= dp[i];
-    else if (L::cy(i) != 0) jy += (CT)L::cy(i) * dp[i];
-  }
+  });
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value, o = L::opp(i);
+    if constexpr (o > i) {
+      acc_add<L::cx(i)>(jx, sx, dp[i]);
+      acc_add<L::cy(i)>(jy, sy, dp[i]);
+    }
+  });
   // FP64 storage holds f, so `drho` is ρ itself and w·drho below is w ρ; deviation storage
   // holds g = f - w, so it is ρ - 1 and w·drho is the deviation w (ρ - 1) of the rest state
   const CT rho = DEV ? (CT)1 + drho : drho;
-  const CT inv = (CT)1 / rho;
+  const CT inv = pair_recip(rho);
   if (has_force) {  // j' = ρ (u + τ F)
-    const CT rs = rho * p.shift;
-    jx += rs * Fx;
-    jy += rs * Fy;
+    jx += rho * sFx;
+    jy += rho * sFy;
   }
-  CT q2 = 0, J2 = 0, inv2 = 0, c3 = 0, c4 = 0, q4 = 0, cs3J2 = 0;
+  // node-wide, weight-free factors of b0, b2, b4 and a3
+  CT D0 = drho, D2 = 0, D4 = 0, J2 = 0, c3 = 0, cs3J2 = 0, csq = 0;
   if constexpr (L::EQ >= 2) {
     J2 = jx * jx + jy * jy;
-    q2 = (p.hcs * J2) * inv;
+    D0 = drho - (p.hcs * J2) * inv;
+    D2 = p.hcs2 * inv;
   }
   if constexpr (L::EQ >= 3) {
-    inv2 = inv * inv;
-    c3 = p.cs * (CT)(1.0 / 6.0) * inv2;  // c / (6 ρ²)
-    cs3J2 = (CT)3 * p.cs * J2;           // 3 c J²
+    c3 = p.cs * (CT)(1.0 / 6.0) * (inv * inv);  // c / (6 ρ²)
+    cs3J2 = (CT)3 * p.cs * J2;                  // 3 c J²
+    csq = p.cs * p.cs;
   }
   if constexpr (L::EQ >= 4) {
-    c4 = (CT)(1.0 / 24.0) * inv2 * inv;  // 1 / (24 ρ³)
-    q4 = (CT)3 * (p.cs * p.cs) * (J2 * J2);
+    const CT c4 = (CT)(1.0 / 24.0) * (inv * inv) * inv;  // 1 / (24 ρ³)
+    D0 += ((CT)3 * csq) * (J2 * J2) * c4;
+    D2 -= ((CT)6 * (csq * p.cs)) * J2 * c4;
+    D4 = (csq * csq) * c4;
   }
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) {
-    const int o = L::opp(i);
-    if (o == i) {
-      CT S = p.w[i] * drho;
-      if constexpr (L::EQ >= 2) S -= p.w[i] * q2;
-      if constexpr (L::EQ >= 4) S += p.w[i] * (q4 * c4);
-      v[i] = ((CT)2 * p.pa_s) * v[i] + p.pom_s * S;
-    } else if (o > i) {
-      CT X = 0;
-      if (L::cx(i) == 1) X += jx;
-      else if (L::cx(i) == -1) X -= jx;
-      else if (L::cx(i) != 0) X += (CT)L::cx(i) * jx;
-      if (L::cy(i) == 1) X += jy;
-      else if (L::cy(i) == -1) X -= jy;
-      else if (L::cy(i) != 0) X += (CT)L::cy(i) * jy;
-      CT S = p.w[i] * drho;
-      const CT X2 = X * X;
-      if constexpr (L::EQ >= 2) S += p.w[i] * ((p.hcs2 * X2) * inv - q2);
-      if constexpr (L::EQ >= 4) {
-        const CT cs2 = p.cs * p.cs;
-        S += p.w[i] * (((cs2 * cs2) * (X2 * X2) - ((CT)6 * (cs2 * p.cs)) * (J2 * X2) + q4) * c4);
+  CT b0[16], b2[16], b4[16], a3[16];
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    if constexpr (class_first<L>(i)) {
+      constexpr int k = vclass<L>(i);
+      b0[k] = p.pws[i] * D0;
+      if constexpr (L::EQ >= 2) b2[k] = p.pws[i] * D2;
+      if constexpr (L::EQ >= 4) b4[k] = p.pws[i] * D4;
+      if constexpr (L::EQ >= 3) a3[k] = (F32 ? p.w[i] : p.pwa[i]) * c3;
+    }
+  });
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value, o = L::opp(i), k = vclass<L>(i);
+    if constexpr (o == i) {
+      v[i] = p.pa_s2 * v[i] + b0[k];
+    } else if constexpr (o > i) {
+      CT X;
+      bool xs = false;
+      acc_add<L::cx(i)>(X, xs, jx);
+      acc_add<L::cy(i)>(X, xs, jy);
+      CT X2 = 0, Se = b0[k];
+      if constexpr (L::EQ >= 2) X2 = X * X;
+      if constexpr (L::EQ >= 4) Se = Se + X2 * (b2[k] + X2 * b4[k]);
+      else if constexpr (L::EQ >= 2) Se = Se + X2 * b2[k];
+      CT Ya;
+      if constexpr (F32) {
+        CT A = p.w1[i] * X;
+        if constexpr (L::EQ >= 3) A += (X * (csq * X2 - cs3J2)) * a3[k];
+        Ya = p.pa_a * dp[i] + p.pom_a * A;
+      } else {
+        CT t = p.pw1a[i];
+        if constexpr (L::EQ >= 3) t += a3[k] * (csq * X2 - cs3J2);
+        Ya = p.pa_a * dp[i] + t * X;
       }
-      CT A = p.w1[i] * X;
-      if constexpr (L::EQ >= 3) A += p.w[i] * ((X * ((p.cs * p.cs) * X2 - cs3J2)) * c3);
-      const CT Ys = p.pa_s * sp[i] + p.pom_s * S;
-      const CT Ya = p.pa_a * dp[i] + p.pom_a * A;
+      const CT Ys = p.pa_s * sp[i] + Se;
       v[i] = Ys + Ya;
       v[o] = Ys - Ya;
     }
-  }
+  });
 }
 
 // Collision of one node in place (v holds f for F64, g = f - w for deviation storage).
@@ -458,87 +490,24 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
 template <class L, class S, int COLL, class CT>
 __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int y, CT* v) {
   constexpr bool DEV = S::DEV;
-  CT Fx = 0, Fy = 0;
-  const bool has_force = p.force_kind != LBM_FORCE_NONE;
-  if (COLL != LBM_ITERATIVE_INIT && has_force) node_force(p, x, y, Fx, Fy);
-  if constexpr (COLL == LBM_MRT) {
-    mrt_collide<L, DEV>(p, v, Fx, Fy, has_force);
-    return;
-  } else if constexpr (COLL == LBM_SRT || COLL == LBM_TRT) {
-    collide_pairs<L, DEV>(p, v, Fx, Fy, has_force);
-    return;
-  } else {
+  if constexpr (COLL == LBM_ITERATIVE_INIT) {
     CT s = v[0];
 #pragma unroll
     for (int i = 1; i < L::Q; ++i) s += v[i];
     const CT rho = DEV ? (CT)1 + s : s;
-    const CT drho = DEV ? s : s;  // only used in deviation form
-    if constexpr (COLL == LBM_ITERATIVE_INIT) {
-      const size_t node = (size_t)y * p.nx + x;
+    const size_t node = (size_t)y * p.nx + x;
 #pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        const CT nl = p.nonlinear[(size_t)i * p.n + node];
-        const CT feq = DEV ? p.w[i] * drho + nl : p.w[i] * rho + nl;
-        v[i] = p.om_a * v[i] + p.om_b * feq;
-      }
-      return;
-    } else {
-      CT jx = 0, jy = 0;
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        if (L::cx(i) == 1) jx += v[i];
-        else if (L::cx(i) == -1) jx -= v[i];
-        else if (L::cx(i) != 0) jx += (CT)L::cx(i) * v[i];
-        if (L::cy(i) == 1) jy += v[i];
-        else if (L::cy(i) == -1) jy -= v[i];
-        else if (L::cy(i) != 0) jy += (CT)L::cy(i) * v[i];
-      }
-      const CT inv_rho = (CT)1 / rho;
-      CT ux = jx * inv_rho, uy = jy * inv_rho;
-      if (has_force) {
-        ux += p.shift * Fx;
-        uy += p.shift * Fy;
-      }
-      const CT usq = ux * ux + uy * uy;
-      CT feq[L::Q];
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        CT cu = 0;
-        if (L::cx(i) == 1) cu += ux;
-        else if (L::cx(i) == -1) cu -= ux;
-        else if (L::cx(i) != 0) cu += (CT)L::cx(i) * ux;
-        if (L::cy(i) == 1) cu += uy;
-        else if (L::cy(i) == -1) cu -= uy;
-        else if (L::cy(i) != 0) cu += (CT)L::cy(i) * uy;
-        // F64: feq = ρ w (1 + P) as the reference forms it.  Deviation storage: geq = feq - w =
-        // w δρ + ρ (w1 c·u + w P_{>=2}), with w1 the first-order coefficients whose second moment
-        // is exactly 1 in the stored precision, so the equilibrium carries exactly the momentum ρu
-        // (rounded weights would give K ρu with K - 1 ~ 1e-8 in FP32, a drift growing with time).
-        if constexpr (DEV) {
-          feq[i] = p.w[i] * drho + rho * (p.w1[i] * cu + p.w[i] * eq_poly_hi<L>(p.cs, cu, usq));
-        } else {
-          const CT P = eq_poly<L>(p.cs, cu, usq);
-          feq[i] = (rho * p.w[i]) * ((CT)1 + P);
-        }
-      }
-      if constexpr (COLL == LBM_SRT) {
-#pragma unroll
-        for (int i = 0; i < L::Q; ++i) v[i] = p.om_a * v[i] + p.om_b * feq[i];
-      } else {  // TRT
-        CT out[L::Q];
-#pragma unroll
-        for (int i = 0; i < L::Q; ++i) {
-          const int o = L::opp(i);
-          const CT feq_s = (CT)0.5 * (feq[i] + feq[o]);
-          const CT feq_a = (CT)0.5 * (feq[i] - feq[o]);
-          const CT f_s = (CT)0.5 * (v[i] + v[o]);
-          const CT f_a = (CT)0.5 * (v[i] - v[o]);
-          out[i] = v[i] + (-p.inv_ts * (f_s - feq_s) - p.inv_ta * (f_a - feq_a));
-        }
-#pragma unroll
-        for (int i = 0; i < L::Q; ++i) v[i] = out[i];
-      }
+    for (int i = 0; i < L::Q; ++i) {
+      const CT nl = p.nonlinear[(size_t)i * p.n + node];
+      const CT feq = DEV ? p.w[i] * s + nl : p.w[i] * rho + nl;
+      v[i] = p.om_a * v[i] + p.om_b * feq;
     }
+  } else {
+    CT sFx = 0, sFy = 0;
+    const bool has_force = p.force_kind != LBM_FORCE_NONE;
+    if (has_force) node_shifted_force(p, x, y, sFx, sFy);
+    if constexpr (COLL == LBM_MRT) mrt_collide<L, DEV>(p, v, sFx, sFy, has_force);
+    else collide_pairs<L, DEV>(p, v, sFx, sFy, has_force);
   }
 }
 
@@ -560,46 +529,28 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
   for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
     const int node = y * p.nx + x;
     if constexpr (COLL == LBM_MRT && MODE != 2) {
-      // streaming form: populations feed the raw moments as they arrive, outputs are rebuilt
-      // and stored one by one, so no per-node array of Q populations stays live
-      CT M[15];
-#pragma unroll
-      for (int k = 0; k < 15; ++k) M[k] = 0;
-      int xw[2 * L::R + 1], yo[2 * L::R + 1];
-      bool near = false;
-      if (MODE != 0) {
-        pull_offsets<L>(p, x, y, xw, yo);
-        near = p.nbc > 0 && (y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R);
-      }
-      auto pop = [&](int i) -> CT {
-        if (MODE == 0) return S::ld(src + (size_t)i * p.n + node);
-        return pop_streamed<L, S>(p, src, x, y, xw, yo, near, i);
-      };
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        const int o = L::opp(i);
-        if (o == i) {
-          M[0] += pop(i);
-        } else if (o > i) {
-          const CT a = pop(i), b = pop(o);
-          mrt_accumulate_pair<L>(M, i, a + b, a - b);
-        }
-      }
-      CT Fx = 0, Fy = 0;
+      // streaming form: populations feed the raw moments as they arrive and the outputs are
+      // rebuilt and stored one by one, so no per-node array of Q populations stays live
+      CT sFx = 0, sFy = 0;
       const bool has_force = p.force_kind != LBM_FORCE_NONE;
-      if (has_force) node_force(p, x, y, Fx, Fy);
-      MrtCoeffs<CT> c;
-      mrt_coeffs<L, S::DEV>(p, M, Fx, Fy, has_force, c);
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        const int o = L::opp(i);
-        if (o == i) {
-          S::st(dst + (size_t)i * p.n + node, p.w[i] * c.B[0]);
-        } else if (o > i) {
-          CT a, b;
-          mrt_out_pair<L, S::DEV>(p, c, i, a, b);
-          S::st(dst + (size_t)i * p.n + node, a);
-          S::st(dst + (size_t)o * p.n + node, b);
+      if (has_force) node_shifted_force(p, x, y, sFx, sFy);
+      auto out = [&](int i, CT val) { S::st(dst + (size_t)i * p.n + node, val); };
+      if constexpr (MODE == 0) {
+        mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
+                            [&](auto I) { return S::ld(src + (size_t)decltype(I)::value * p.n + node); }, out);
+      } else {
+        int xw[2 * L::R + 1], yo[2 * L::R + 1];
+        pull_offsets<L>(p, x, y, xw, yo);
+        const bool near = p.nbc > 0 && (y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R);
+        if (near) {
+          mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
+                              [&](auto I) { return pop_streamed<L, S>(p, src, x, y, xw, yo, true, decltype(I)::value); },
+                              out);
+        } else {
+          mrt_node<L, S::DEV>(p, sFx, sFy, has_force, [&](auto I) {
+            constexpr int i = decltype(I)::value;
+            return S::ld(src + (size_t)i * p.n + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
+          }, out);
         }
       }
     } else {

@@ -38,16 +38,17 @@ def test_adjoint_matches_finite_differences(lbm_gpu):
     prob = _setup(lbm, tau_s=tau_s, F=F)
     res = prob.run(u0, ut)
     prob.close()
-    h = 1e-6
-    fd_ts = (_loss(lbm, u0, ut, tau_s + h, tau_a, F) - _loss(lbm, u0, ut, tau_s - h, tau_a, F)) / (2 * h)
-    fd_ta = (_loss(lbm, u0, ut, tau_s, tau_a + h, F) - _loss(lbm, u0, ut, tau_s, tau_a - h, F)) / (2 * h)
-    hF = 1e-7
-    fd_fx = (_loss(lbm, u0, ut, tau_s, tau_a, (F[0] + hF, F[1])) -
-             _loss(lbm, u0, ut, tau_s, tau_a, (F[0] - hF, F[1]))) / (2 * hF)
+    # fourth-order central differences: the loss is ~0.2, so a two-point difference with a step
+    # of 1e-6 carries a rounding error of ~1e-11, the size of the smallest gradients checked here
+    def fd(fun, h):
+        return (fun(-2 * h) - 8 * fun(-h) + 8 * fun(h) - fun(2 * h)) / (12 * h)
+
+    fd_ts = fd(lambda e: _loss(lbm, u0, ut, tau_s + e, tau_a, F), 1e-4)
+    fd_ta = fd(lambda e: _loss(lbm, u0, ut, tau_s, tau_a + e, F), 1e-4)
+    fd_fx = fd(lambda e: _loss(lbm, u0, ut, tau_s, tau_a, (F[0] + e, F[1])), 1e-7)
     rng = np.random.default_rng(7)
     v = rng.normal(size=u0.shape)
-    hu = 1e-6
-    fd_u = (_loss(lbm, u0 + hu * v, ut, tau_s, tau_a, F) - _loss(lbm, u0 - hu * v, ut, tau_s, tau_a, F)) / (2 * hu)
+    fd_u = fd(lambda e: _loss(lbm, u0 + e * v, ut, tau_s, tau_a, F), 1e-5)
     for ad, fd in [(res["dtau_s"], fd_ts), (res["dtau_a"], fd_ta), (res["dF"][0], fd_fx),
                    (float(np.sum(res["grad_u0"] * v)), fd_u)]:
         assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-12), (ad, fd)
