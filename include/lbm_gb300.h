@@ -219,6 +219,15 @@ int32_t lbm_batch_set_stream(lbm_batch* batch, void* stream);
 int32_t lbm_batch_synchronize(lbm_batch* batch);
 int64_t lbm_batch_last_launch_count(const lbm_batch* batch);
 const char* lbm_batch_last_error(const lbm_batch* batch);
+/* The stop criteria's reductions for many members at once (the per-member next! checks of a
+ * sweep, stopping_criteria.jl:17-115): kind LBM_REDUCE_MEAN_VELOCITY, _VELOCITY_CONVERGENCE or
+ * _CONSERVED over the members with select[k] != 0 (select NULL: all); out holds count x 16
+ * doubles, row k being what lbm_reduce(member k, kind) returns (zeros for members not selected;
+ * CONSERVED: row k[3] counts non-finite populations instead of failing).  Synchronous. */
+int32_t lbm_batch_reduce(lbm_batch* batch, int32_t kind, const uint8_t* select, double* out);
+/* Members issue their own calls on the batch's stream until the batch is destroyed (no ordering
+ * between streams per batch call; members must outlive the batch). */
+int32_t lbm_batch_share_stream(lbm_batch* batch);
 
 /* ---- adjoint (reverse-mode gradients) -----------------------------------------------------
  * No differentiation exists in the reference; this is the discrete adjoint of the fused step

@@ -36,9 +36,11 @@ from .processing_methods import (ProcessingMethod, TrackHydrodynamicErrors, Comp
                                  NoStoppingCriteria, MeanVelocityStoppingCriteria, VelocityConvergenceStoppingCriteria,
                                  DensityConvergence, TrackRow, CompareRow, track_errors)
 from .device import DeviceLattice, DeviceBatch
-from .model import LatticeBoltzmannModel, simulate, simulate_model, run_steps, collide, stream, apply
+from .model import (LatticeBoltzmannModel, simulate, simulate_model, simulate_batch, run_steps, collide, stream,
+                    apply)
 from . import build_native
-from .studies import tgv_instances, run_tgv_study, convergence_order
+from .studies import (tgv_instances, run_tgv_study, convergence_order, trt_sweep_points, julia_range,
+                      build_trt_sweep_models, run_trt_sweep)
 from .adjoint import AdjointProblem, divergence_free_field, trt_magic, magic_total_derivative, LBMLoss
 
 StopCriteria = StopCriteriaFor

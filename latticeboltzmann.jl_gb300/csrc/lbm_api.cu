@@ -21,9 +21,12 @@
 using namespace lbm;
 
 namespace lbm {
-cudaError_t batch_launch(int storage, int coll, int qid, const void* members, int nactive, long long blocks,
-                         long long t, cudaStream_t s);
-size_t batch_member_size(int storage);
+cudaError_t batch_launch(int storage, int coll, int qid, const void* statics, const BatchDyn* dyn, int nactive,
+                         long long blocks, long long t, cudaStream_t s);
+cudaError_t batch_reduce_launch(int storage, int qid, int K, const void* statics, const ReduceArgs* args,
+                                const BatchDyn* dyn, int nmem, long long blocks, double* partial, long long part_base,
+                                double* out, cudaStream_t s);
+size_t batch_static_size(int storage);
 struct AdjArgs;
 cudaError_t adj_launch(int op, int qid, int storage, int coll, const void* params, AdjArgs a, const void* src, int pull,
                        const void* lam_next, void* lam_out, double* slots, int nblocks, const double* u0,
@@ -842,14 +845,22 @@ struct lbm_batch {
   std::vector<lbm_ctx*> members;
   int device = 0, storage = 0, coll = 0;
   cudaStream_t own_stream = nullptr, stream = nullptr;
-  void* d_members = nullptr;      // device array of BatchMember<CT>
-  void* h_members = nullptr;      // pinned staging copy
-  size_t member_bytes = 0;
+  void* d_static = nullptr;       // BatchStatic<CT> per member, uploaded once
+  BatchDyn* d_dyn = nullptr;      // per call, launch order
+  BatchDyn* h_dyn = nullptr;      // pinned staging copy
+  cudaEvent_t staged = nullptr;   // the last upload from h_dyn has completed
+  ReduceArgs* d_rargs = nullptr;  // per member, set up by the first reduction
+  double* d_rpartial = nullptr;
+  long long rpartial_blocks = 0;
+  double* d_rout = nullptr;       // count x kRedMaxK
+  double* h_rout = nullptr;       // pinned
   cudaEvent_t done = nullptr;
   cudaGraphExec_t graph = nullptr;
   std::vector<int64_t> graph_key;  // sorted step counts the graph was captured for
   std::vector<int> graph_order;
+  int64_t graph_launches = 0;
   int64_t last_launches = 0;
+  bool shared = false;             // the members issue their own work on the batch's stream
   std::string err;
 };
 
@@ -861,15 +872,47 @@ int bfail(lbm_batch* b, int status, const std::string& msg) {
 }
 
 template <class CT>
-void fill_member(BatchMember<CT>& m, const StepParams<CT>& p, lbm_ctx* c, int64_t steps, long long block_start) {
+void fill_static(BatchStatic<CT>& m, const StepParams<CT>& p, const lbm_ctx* c) {
   m.p = p;
   m.buf0 = c->buf[0];
   m.buf1 = c->buf[1];
-  m.qid = c->qid;
-  m.cur0 = c->cur;
-  m.phase0 = c->phase;
-  m.steps = steps;
-  m.block_start = block_start;
+}
+
+// The batch stream waits for the members' own streams (uploads and reductions issued there),
+// once per distinct stream.
+int batch_wait_members(lbm_batch* b) {
+  std::vector<cudaStream_t> seen;
+  for (lbm_ctx* c : b->members) {
+    if (c->stream == b->stream || std::find(seen.begin(), seen.end(), c->stream) != seen.end()) continue;
+    seen.push_back(c->stream);
+    if (cudaEventRecord(b->done, c->stream) != cudaSuccess || cudaStreamWaitEvent(b->stream, b->done, 0) != cudaSuccess)
+      return bfail(b, LBM_ERR_CUDA, "ordering member streams");
+  }
+  return LBM_OK;
+}
+
+// The members' streams wait for the batch's work, once per distinct stream.
+int batch_release_members(lbm_batch* b) {
+  if (cudaEventRecord(b->done, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "event");
+  std::vector<cudaStream_t> seen;
+  for (lbm_ctx* c : b->members) {
+    if (c->stream == b->stream || std::find(seen.begin(), seen.end(), c->stream) != seen.end()) continue;
+    seen.push_back(c->stream);
+    if (cudaStreamWaitEvent(c->stream, b->done, 0) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "member wait");
+  }
+  return LBM_OK;
+}
+
+// Uploads dyn[0..count) through the pinned staging buffer (waiting for the previous upload from
+// it to finish before it is overwritten).
+int batch_upload_dyn(lbm_batch* b, const std::vector<BatchDyn>& dyn) {
+  if (cudaEventSynchronize(b->staged) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "staging wait");
+  std::copy(dyn.begin(), dyn.end(), b->h_dyn);
+  if (cudaMemcpyAsync(b->d_dyn, b->h_dyn, sizeof(BatchDyn) * dyn.size(), cudaMemcpyHostToDevice, b->stream) !=
+          cudaSuccess ||
+      cudaEventRecord(b->staged, b->stream) != cudaSuccess)
+    return bfail(b, LBM_ERR_CUDA, "descriptor upload");
+  return LBM_OK;
 }
 
 }  // namespace
@@ -894,12 +937,25 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
   b->device = c0->device;
   b->storage = c0->storage;
   b->coll = c0->coll;
-  b->member_bytes = batch_member_size(b->storage);
   cudaSetDevice(b->device);
+  const size_t sb = batch_static_size(b->storage);
+  std::vector<char> h(sb * count);
+  for (int k = 0; k < count; ++k) {
+    const lbm_ctx* c = members[k];
+    char* slot = h.data() + k * sb;
+    if (b->storage == LBM_STORE_F64) fill_static(*reinterpret_cast<BatchStatic<double>*>(slot), c->pd, c);
+    else if (b->storage == LBM_STORE_DF64_DEV) fill_static(*reinterpret_cast<BatchStatic<dd>*>(slot), c->px, c);
+    else fill_static(*reinterpret_cast<BatchStatic<float>*>(slot), c->pf, c);
+  }
   if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
-      cudaMalloc(&b->d_members, b->member_bytes * count) != cudaSuccess ||
-      cudaMallocHost(&b->h_members, b->member_bytes * count) != cudaSuccess) {
+      cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMalloc(&b->d_static, sb * count) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_dyn, sizeof(BatchDyn) * count) != cudaSuccess ||
+      cudaMallocHost((void**)&b->h_dyn, sizeof(BatchDyn) * count) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_rout, sizeof(double) * kRedMaxK * count) != cudaSuccess ||
+      cudaMallocHost((void**)&b->h_rout, sizeof(double) * kRedMaxK * count) != cudaSuccess ||
+      cudaMemcpy(b->d_static, h.data(), sb * count, cudaMemcpyHostToDevice) != cudaSuccess) {
     lbm_batch_destroy(b);
     return LBM_ERR_NOMEM;
   }
@@ -912,10 +968,19 @@ void lbm_batch_destroy(lbm_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->shared)
+    for (lbm_ctx* c : b->members)
+      if (c->stream == b->stream) c->stream = c->own_stream;
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  cudaFree(b->d_members);
-  if (b->h_members) cudaFreeHost(b->h_members);
+  cudaFree(b->d_static);
+  cudaFree(b->d_dyn);
+  cudaFree(b->d_rargs);
+  cudaFree(b->d_rpartial);
+  cudaFree(b->d_rout);
+  if (b->h_dyn) cudaFreeHost(b->h_dyn);
+  if (b->h_rout) cudaFreeHost(b->h_rout);
   if (b->done) cudaEventDestroy(b->done);
+  if (b->staged) cudaEventDestroy(b->staged);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
 }
@@ -927,12 +992,31 @@ int32_t lbm_batch_set_stream(lbm_batch* b, void* stream) {
   if (!b) return LBM_ERR_INVALID;
   cudaSetDevice(b->device);
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "stream synchronize");
-  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  if (b->shared)
+    for (lbm_ctx* c : b->members)
+      if (c->stream == b->stream) c->stream = next;
+  b->stream = next;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     b->graph_key.clear();
   }
+  return LBM_OK;
+}
+
+// Every member issues its own work (uploads, reductions, downloads) on the batch's stream from
+// now on, so batch calls need no ordering between streams; the members get their own streams
+// back when the batch is destroyed.
+int32_t lbm_batch_share_stream(lbm_batch* b) {
+  if (!b) return LBM_ERR_INVALID;
+  cudaSetDevice(b->device);
+  for (lbm_ctx* c : b->members) {
+    if (c->stream == b->stream) continue;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "member synchronize");
+    c->stream = b->stream;
+  }
+  b->shared = true;
   return LBM_OK;
 }
 
@@ -943,7 +1027,7 @@ int32_t lbm_batch_synchronize(lbm_batch* b) {
 }
 
 // Every member k advances nsteps[k] steps.  All members' steps are issued as ONE CUDA graph of
-// kernels, one per global step, each covering every member still running at that step.
+// kernels, one per global step and velocity set, each covering every member still running.
 int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
   if (!b || !nsteps) return LBM_ERR_INVALID;
   cudaSetDevice(b->device);
@@ -961,41 +1045,32 @@ int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
     return qa != qc ? qa < qc : nsteps[a] > nsteps[c];
   });
   std::vector<int64_t> key(count);
-  std::vector<long long> start(count, 0), end(count, 0);  // block range of each member in its group
-  std::vector<int> group_begin;  // first rank of each velocity-set group
+  std::vector<long long> end(count, 0);  // end of each member's block range in its group
+  std::vector<int> group_begin;          // first rank of each velocity-set group
+  std::vector<BatchDyn> dyn(count);
   for (int r = 0; r < count; ++r) {
     const lbm_ctx* c = b->members[order[r]];
     key[r] = nsteps[order[r]];
     const bool first = r == 0 || b->members[order[r - 1]]->qid != c->qid;
     if (first) group_begin.push_back(r);
-    start[r] = first ? 0 : end[r - 1];
-    end[r] = start[r] + (c->n + kBlockX - 1) / kBlockX;
+    BatchDyn& d = dyn[r];
+    d.block_start = first ? 0 : end[r - 1];
+    d.steps = key[r];
+    d.member = order[r];
+    d.cur0 = c->cur;
+    d.phase0 = c->phase == POST_COLLIDE ? 1 : 0;
+    d.pad = 0;
+    end[r] = d.block_start + (c->n + kBlockX - 1) / kBlockX;
   }
   group_begin.push_back(count);
   int64_t tmax = 0;
   for (int r = 0; r < count; ++r) tmax = std::max(tmax, key[r]);
   b->last_launches = 0;
   if (tmax == 0) return LBM_OK;
-  // the members' own pending work (uploads, reductions) precedes the batch
-  for (lbm_ctx* c : b->members) {
-    if (cudaEventRecord(b->done, c->stream) != cudaSuccess || cudaStreamWaitEvent(b->stream, b->done, 0) != cudaSuccess)
-      return bfail(b, LBM_ERR_CUDA, "ordering member streams");
-  }
-  // member descriptors (parameters, buffers, current parity and phase) for this call
-  char* h = static_cast<char*>(b->h_members);
-  for (int r = 0; r < count; ++r) {
-    lbm_ctx* c = b->members[order[r]];
-    char* slot = h + r * b->member_bytes;
-    if (b->storage == LBM_STORE_F64)
-      fill_member(*reinterpret_cast<BatchMember<double>*>(slot), c->pd, c, key[r], start[r]);
-    else if (b->storage == LBM_STORE_DF64_DEV)
-      fill_member(*reinterpret_cast<BatchMember<dd>*>(slot), c->px, c, key[r], start[r]);
-    else
-      fill_member(*reinterpret_cast<BatchMember<float>*>(slot), c->pf, c, key[r], start[r]);
-  }
-  if (cudaMemcpyAsync(b->d_members, b->h_members, b->member_bytes * count, cudaMemcpyHostToDevice, b->stream) !=
-      cudaSuccess)
-    return bfail(b, LBM_ERR_CUDA, "descriptor upload");
+  int rc = batch_wait_members(b);
+  if (rc) return rc;
+  rc = batch_upload_dyn(b, dyn);
+  if (rc) return rc;
   if (!b->graph || b->graph_key != key || b->graph_order != order) {
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);
@@ -1008,14 +1083,15 @@ int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
     const int ngroups = (int)group_begin.size() - 1;
     std::vector<int> nactive(ngroups);
     for (int gi = 0; gi < ngroups; ++gi) nactive[gi] = group_begin[gi + 1] - group_begin[gi];
+    int64_t launches = 0;
     for (int64_t t = 0; t < tmax && e == cudaSuccess; ++t) {
       for (int gi = 0; gi < ngroups && e == cudaSuccess; ++gi) {
         const int g0 = group_begin[gi];
         while (nactive[gi] > 0 && key[g0 + nactive[gi] - 1] <= t) --nactive[gi];
         if (nactive[gi] == 0) continue;
-        const char* base = static_cast<const char*>(b->d_members) + (size_t)g0 * b->member_bytes;
-        e = batch_launch(b->storage, b->coll, b->members[order[g0]]->qid, base, nactive[gi],
+        e = batch_launch(b->storage, b->coll, b->members[order[g0]]->qid, b->d_static, b->d_dyn + g0, nactive[gi],
                          end[g0 + nactive[gi] - 1], t, b->stream);
+        ++launches;
       }
     }
     cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
@@ -1031,22 +1107,112 @@ int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
     }
     b->graph_key = key;
     b->graph_order = order;
+    b->graph_launches = launches;
   }
   if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "graph launch");
-  b->last_launches = tmax;
+  b->last_launches = b->graph_launches;
   // members continue after the batch: advance their parity / phase and order their streams
-  if (cudaEventRecord(b->done, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "event");
   for (int k = 0; k < count; ++k) {
     lbm_ctx* c = b->members[k];
     if (nsteps[k] > 0) {
       c->cur = (int)((c->cur + nsteps[k]) & 1);
       c->phase = POST_COLLIDE;
     }
-    if (cudaStreamWaitEvent(c->stream, b->done, 0) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "member wait");
   }
-  return LBM_OK;
+  return batch_release_members(b);
 }
 
+// The reductions lbm_reduce computes without analytic fields (MEAN_VELOCITY,
+// VELOCITY_CONVERGENCE, CONSERVED) for every member at once: out[k * 16 + j] is what
+// lbm_reduce(member k, kind) would return in out[j].  One launch per velocity set plus one
+// fixed-order finish; VELOCITY_CONVERGENCE updates each member's previous-velocity planes as
+// lbm_reduce does.  CONSERVED reports the non-finite population count in out[k * 16 + 3].
+int32_t lbm_batch_reduce(lbm_batch* b, int32_t kind, const uint8_t* select, double* out) {
+  if (!b || !out) return LBM_ERR_INVALID;
+  if (kind != LBM_REDUCE_MEAN_VELOCITY && kind != LBM_REDUCE_VELOCITY_CONVERGENCE && kind != LBM_REDUCE_CONSERVED)
+    return bfail(b, LBM_ERR_UNSUPPORTED, "batched reductions: MEAN_VELOCITY, VELOCITY_CONVERGENCE, CONSERVED");
+  cudaSetDevice(b->device);
+  const int count = (int)b->members.size();
+  for (lbm_ctx* c : b->members)
+    if (!c->have_state) return bfail(b, LBM_ERR_STATE, "member without uploaded state");
+  int rc = batch_wait_members(b);
+  if (rc) return rc;
+  if (!b->d_rargs) {  // per-member reduction arguments (weights, 1/c_s², previous-velocity planes)
+    std::vector<ReduceArgs> ra(count);
+    for (int k = 0; k < count; ++k) {
+      lbm_ctx* c = b->members[k];
+      if (!c->d_uold) {
+        if (ensure(c, &c->d_uold, (size_t)c->n * 2 * sizeof(double))) return bfail(b, LBM_ERR_NOMEM, c->err);
+        if (cudaMemsetAsync(c->d_uold, 0, (size_t)c->n * 2 * sizeof(double), b->stream) != cudaSuccess)
+          return bfail(b, LBM_ERR_CUDA, "previous-velocity planes");
+      }
+      ra[k] = c->red;
+      ra[k].u_old = c->d_uold;
+    }
+    if (cudaMalloc((void**)&b->d_rargs, sizeof(ReduceArgs) * count) != cudaSuccess)
+      return bfail(b, LBM_ERR_NOMEM, "reduction arguments");
+    if (cudaMemcpy(b->d_rargs, ra.data(), sizeof(ReduceArgs) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+      return bfail(b, LBM_ERR_CUDA, "reduction arguments");
+  }
+  const int K = red_kind_k(kind);
+  std::vector<int> order;
+  for (int k = 0; k < count; ++k)
+    if (!select || select[k]) order.push_back(k);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int c) { return b->members[a]->qid < b->members[c]->qid; });
+  const int nsel = (int)order.size();
+  std::fill(out, out + (size_t)count * kRedMaxK, 0.0);
+  if (nsel == 0) return LBM_OK;
+  std::vector<BatchDyn> dyn(nsel);
+  std::vector<int> group_begin;
+  std::vector<long long> group_base;  // first partial block of each group
+  long long total = 0, gstart = 0;
+  for (int r = 0; r < nsel; ++r) {
+    const lbm_ctx* c = b->members[order[r]];
+    const bool first = r == 0 || b->members[order[r - 1]]->qid != c->qid;
+    if (first) {
+      group_begin.push_back(r);
+      group_base.push_back(total);
+      gstart = 0;
+    }
+    const long long nb = c->red_blocks;  // lbm_reduce's partition, so the sums are bitwise the same
+    BatchDyn& d = dyn[r];
+    d.block_start = gstart;
+    d.steps = nb;
+    d.member = order[r];
+    d.cur0 = c->cur;
+    d.phase0 = c->phase == POST_COLLIDE ? 1 : 0;
+    d.pad = 0;
+    gstart += nb;
+    total += nb;
+  }
+  group_begin.push_back(nsel);
+  if (total > b->rpartial_blocks) {
+    cudaFree(b->d_rpartial);
+    b->d_rpartial = nullptr;
+    if (cudaMalloc((void**)&b->d_rpartial, sizeof(double) * kRedMaxK * total) != cudaSuccess) {
+      b->rpartial_blocks = 0;
+      return bfail(b, LBM_ERR_NOMEM, "reduction partials");
+    }
+    b->rpartial_blocks = total;
+  }
+  rc = batch_upload_dyn(b, dyn);
+  if (rc) return rc;
+  for (size_t gi = 0; gi + 1 < group_begin.size(); ++gi) {
+    const int g0 = group_begin[gi], n = group_begin[gi + 1] - g0;
+    const long long blocks = dyn[group_begin[gi + 1] - 1].block_start + dyn[group_begin[gi + 1] - 1].steps;
+    cudaError_t e = batch_reduce_launch(b->storage, b->members[order[g0]]->qid, K, b->d_static, b->d_rargs,
+                                        b->d_dyn + g0, n, blocks, b->d_rpartial, group_base[gi], b->d_rout, b->stream);
+    if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("batched reduction: ") + cudaGetErrorString(e));
+  }
+  if (cudaMemcpyAsync(b->h_rout, b->d_rout, sizeof(double) * kRedMaxK * count, cudaMemcpyDeviceToHost, b->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return bfail(b, LBM_ERR_CUDA, "batched reduction result");
+  for (int k : order)
+    for (int j = 0; j < K; ++j) out[(size_t)k * kRedMaxK + j] = b->h_rout[(size_t)k * kRedMaxK + j];
+  return batch_release_members(b);
+}
 
 }  // extern "C"
 

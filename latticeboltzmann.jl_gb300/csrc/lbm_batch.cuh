@@ -11,23 +11,40 @@
 // and ping-pong parity; the graph holds one kernel node per global step.
 #pragma once
 
-#include "lbm_step.cuh"
+#include "lbm_reduce.cuh"
 
 namespace lbm {
 
 constexpr int kBatchMax = 65536;  // members per batch
 
+// What stays fixed for a member over the batch's life: parameters and buffers.
 template <class CT>
-struct BatchMember {
+struct BatchStatic {
   StepParams<CT> p;
-  void* buf0;            // member buffers (the member context owns them)
+  void* buf0;  // member buffers (the member context owns them)
   void* buf1;
-  int qid;
-  int cur0;              // buffer holding the member's state when the batch starts
-  int phase0;            // 0: f_stream resident (first step collides only), 1: post-collision
-  long long steps;       // steps this member takes
-  long long block_start; // first global block index of the member (prefix sum)
 };
+
+// Per call, in launch order (members grouped by velocity set, descending step count).
+struct BatchDyn {
+  long long block_start;  // first block of the member within its group (prefix sum)
+  long long steps;        // steps this member takes (stepping) / its block count (reductions)
+  int member;             // index into the static array
+  int cur0;               // buffer holding the member's state when the call starts
+  int phase0;             // 0: f_stream resident (no pull, a first step collides only), 1: post-collision
+  int pad;
+};
+
+// Last member of the first n whose block_start <= b (block_start is ascending).
+__device__ __forceinline__ int batch_find(const BatchDyn* __restrict__ dyn, int n, long long b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (dyn[mid].block_start <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
 
 template <class L, class S, int COLL>
 __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>& p, const typename S::T* src,
@@ -46,27 +63,63 @@ __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>&
 // run in their own launch of the same step).  A block covers kBlockX consecutive nodes (x
 // fastest) of one member, so lattices of a few nodes use a few threads, not a row of blocks.
 template <class L, class S, int COLL>
-__global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchMember<typename S::C>* __restrict__ members,
-                                                             int nactive, long long t) {
+__global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchStatic<typename S::C>* __restrict__ statics,
+                                                             const BatchDyn* __restrict__ dyn, int nactive,
+                                                             long long t) {
   using T = typename S::T;
   const long long b = blockIdx.x;
-  int lo = 0, hi = nactive - 1;
-  while (lo < hi) {  // last member whose block_start <= b
-    const int mid = (lo + hi + 1) >> 1;
-    if (members[mid].block_start <= b) lo = mid;
-    else hi = mid - 1;
-  }
-  const BatchMember<typename S::C>& m = members[lo];
+  const BatchDyn& d = dyn[batch_find(dyn, nactive, b)];
+  const BatchStatic<typename S::C>& m = statics[d.member];
   const StepParams<typename S::C>& p = m.p;
-  const long long node = (b - m.block_start) * kBlockX + threadIdx.x;
+  const long long node = (b - d.block_start) * kBlockX + threadIdx.x;
   if (node >= p.n) return;
   const int y = (int)(node / p.nx);
   const int x = (int)(node - (long long)y * p.nx);
-  const int parity = (int)((m.cur0 + t) & 1);
+  const int parity = (int)((d.cur0 + t) & 1);
   const T* src = static_cast<const T*>(parity ? m.buf1 : m.buf0);
   T* dst = static_cast<T*>(parity ? m.buf0 : m.buf1);
-  const bool local = (t == 0) && (m.phase0 == 0);
+  const bool local = (t == 0) && (d.phase0 == 0);
   batch_node_step<L, S, COLL>(p, src, dst, x, y, local);
+}
+
+// Reductions of many members in one launch: member d.member owns d.steps consecutive blocks
+// (from d.block_start), each block writes one partial of K sums, and batch_reduce_finish adds a
+// member's partials in block order (deterministic).  The observed state is pulled (with the
+// boundary rules) when the member holds its post-collision array.
+template <class L, class S, int K>
+__global__ void __launch_bounds__(kRedThreads) batch_reduce_kernel(const BatchStatic<typename S::C>* __restrict__ statics,
+                                                                   const ReduceArgs* __restrict__ args,
+                                                                   const BatchDyn* __restrict__ dyn, int nmem,
+                                                                   double* __restrict__ partial) {
+  using T = typename S::T;
+  const long long b = blockIdx.x;
+  const BatchDyn& d = dyn[batch_find(dyn, nmem, b)];
+  const BatchStatic<typename S::C>& m = statics[d.member];
+  const ReduceArgs& r = args[d.member];
+  const T* src = static_cast<const T*>(d.cur0 ? m.buf1 : m.buf0);
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  const long long first = (b - d.block_start) * kRedThreads + threadIdx.x;
+  const long long stride = d.steps * kRedThreads;
+  for (long long node = first; node < m.p.n; node += stride) {
+    const int y = (int)(node / m.p.nx), x = (int)(node - (long long)y * m.p.nx);
+    if (d.phase0) reduce_node<L, S, true, K>(m.p, r, src, x, y, node, acc);
+    else reduce_node<L, S, false, K>(m.p, r, src, x, y, node, acc);
+  }
+  block_reduce_store<K>(acc, partial);
+}
+
+template <int K>
+__global__ void batch_reduce_finish(const BatchDyn* __restrict__ dyn, int nmem, const double* __restrict__ partial,
+                                    long long part_base, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nmem * K) return;
+  const int r = i / K, k = i - r * K;
+  const BatchDyn& d = dyn[r];
+  double s = 0.0;
+  for (long long bb = 0; bb < d.steps; ++bb) s += partial[(size_t)(part_base + d.block_start + bb) * K + k];
+  out[(size_t)d.member * kRedMaxK + k] = s;
 }
 
 }  // namespace lbm

@@ -58,12 +58,16 @@ __device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
 
 __device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
 
+// The product is left as the pair (p, e) with p = fl(a.hi b.hi) and e the rounding error of
+// p plus the cross terms, |e| <= ~2^-22 |p|, without the closing fast_two_sum: every consumer
+// (two_sum-based addition, another product, the reciprocal, a store) is exact or error-free
+// in its leading part for such a pair, and the renormalisation happens in the next addition.
 __device__ __forceinline__ dd operator*(dd a, dd b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  return fast_two_sum(p, e);
+  return dd(p, e);
 }
 
 // 1 / b: float reciprocal refined by one Newton step r + r (1 - b r) in float-float

@@ -58,18 +58,13 @@ __device__ __forceinline__ void node_f64(const StepParams<typename S::C>& p, con
   for (int i = 0; i < L::Q; ++i) f[i] = S::DEV ? r.w[i] + (double)v[i] : (double)v[i];
 }
 
+// The contribution of node (x, y) to the K sums of one reduction kind.
 template <class L, class S, bool PULL, int K>
-__global__ void __launch_bounds__(kRedThreads) reduce_kernel(StepParams<typename S::C> p, ReduceArgs r,
-                                                             const typename S::T* __restrict__ src,
-                                                             double* __restrict__ partial) {
-  double acc[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) acc[k] = 0.0;
-  const long long total = p.n;
-  const double ics = 1.0 / r.cs;
-  for (long long node = (long long)blockIdx.x * kRedThreads + threadIdx.x; node < total;
-       node += (long long)gridDim.x * kRedThreads) {
-    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+__device__ __forceinline__ void reduce_node(const StepParams<typename S::C>& p, const ReduceArgs& r,
+                                            const typename S::T* __restrict__ src, int x, int y, long long node,
+                                            double (&acc)[K]) {
+  {
+    const double ics = 1.0 / r.cs;
     double f[L::Q];
     node_f64<L, S, PULL>(p, r, src, x, y, f);
     double rho = f[0];
@@ -171,6 +166,20 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(StepParams<typename
       for (int i = 0; i < L::Q; ++i) bad += isfinite(f[i]) ? 0 : 1;
       acc[3] += bad;
     }
+  }
+}
+
+template <class L, class S, bool PULL, int K>
+__global__ void __launch_bounds__(kRedThreads) reduce_kernel(StepParams<typename S::C> p, ReduceArgs r,
+                                                             const typename S::T* __restrict__ src,
+                                                             double* __restrict__ partial) {
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (long long node = (long long)blockIdx.x * kRedThreads + threadIdx.x; node < p.n;
+       node += (long long)gridDim.x * kRedThreads) {
+    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+    reduce_node<L, S, PULL, K>(p, r, src, x, y, node, acc);
   }
   block_reduce_store<K>(acc, partial);
 }

@@ -461,8 +461,8 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
       bool xs = false;
       acc_add<L::cx(i)>(X, xs, jx);
       acc_add<L::cy(i)>(X, xs, jy);
-      CT X2 = 0, Se = b0[k];
-      if constexpr (L::EQ >= 2) X2 = X * X;
+      [[maybe_unused]] const CT X2 = X * X;
+      CT Se = b0[k];
       if constexpr (L::EQ >= 4) Se = Se + X2 * (b2[k] + X2 * b4[k]);
       else if constexpr (L::EQ >= 2) Se = Se + X2 * b2[k];
       CT Ya;

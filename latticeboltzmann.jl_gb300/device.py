@@ -108,6 +108,7 @@ class DeviceLattice:
             raise N.LbmError(st, f"lbm_create: {L.lbm_status_string(st).decode()}")
         self.h = h
         self._keep = []  # the library copied what it needs
+        self.prefetched = {}  # reduction kind -> sums supplied by a batched reduction
 
     # ---- lifetime ----------------------------------------------------------------------
     def close(self):
@@ -155,6 +156,9 @@ class DeviceLattice:
 
     # ---- reductions --------------------------------------------------------------------
     def reduce(self, kind, fields=None, tau=0.0, u_max=1.0, area=0.0):
+        pre = self.prefetched.pop(kind, None) if fields is None else None
+        if pre is not None:  # computed for this lattice by a batched reduction (simulate_batch)
+            return pre
         out = np.zeros(16)
         an = None
         keep = []
@@ -239,6 +243,24 @@ class DeviceBatch:
 
     def last_launch_count(self) -> int:
         return int(N.lib().lbm_batch_last_launch_count(self.h))
+
+    def reduce(self, kind, select=None):
+        """lbm_batch_reduce: the (members, K) sums of a stop-criterion reduction of the selected
+        members (all when select is None; rows of unselected members are zero)."""
+        out = np.zeros((len(self.lattices), 16))
+        sel = None
+        if select is not None:
+            sel = np.ascontiguousarray(select, dtype=np.uint8)
+            if sel.shape != (len(self.lattices),):
+                raise ValueError("one select flag per member")
+        self._check(N.lib().lbm_batch_reduce(self.h, int(kind),
+                                             sel.ctypes.data_as(C.POINTER(C.c_uint8)) if sel is not None else None,
+                                             out.ctypes.data_as(N._DP)))
+        return out[:, : N.REDUCE_K[kind]]
+
+    def share_stream(self):
+        """lbm_batch_share_stream: members issue their own work on the batch's stream."""
+        self._check(N.lib().lbm_batch_share_stream(self.h))
 
     def close(self):
         if getattr(self, "h", None):

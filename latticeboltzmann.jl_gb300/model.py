@@ -123,6 +123,76 @@ def simulate_model(model, time):
     return model
 
 
+def simulate_batch(models, times):
+    """simulate(model, time) (lattice_boltzmann_model.jl:60-77) for many models at once, e.g. the
+    points of a parameter sweep or a convergence study.  Each model follows exactly the loop of
+    simulate_model -- its own steps, its own next! events, its own stop -- but the members step
+    together through one DeviceBatch (one CUDA graph per round, one kernel per global step), and
+    the stop criteria's reductions of all members due at a round come from one batched
+    reduction.  `times` is one range / (first, last) pair for all models or one per model."""
+    from .device import DeviceBatch
+    models = list(models)
+    n = len(models)
+    if isinstance(times, (range, tuple)):
+        times = [times] * n
+    bounds = [_time_bounds(tm) for tm in times]
+    t = [b[0] for b in bounds]
+    last = [b[1] for b in bounds]
+    pms = [m.processing_method for m in models]
+    batch = DeviceBatch([m.lattice for m in models])
+    batch.share_stream()
+    stage = ["loop"] * n  # loop -> final (the last next!) -> done
+    try:
+        while True:
+            nsteps = np.zeros(n, dtype=np.int64)
+            events = [None] * n
+            for k in range(n):
+                if stage[k] != "loop":
+                    continue
+                if t[k] > last[k]:
+                    stage[k] = "final"
+                    continue
+                ev = pms[k].next_event(t[k] + 1)
+                nsteps[k] = last[k] - t[k] + 1 if ev is None or ev > last[k] + 1 else max(1, ev - t[k])
+                events[k] = ev
+            if nsteps.any():  # (batches hold no time-dependent force, so the steps need no time)
+                batch.step(nsteps)
+            # members at an event (or at their final next!) and the stop reductions they will ask for
+            acting = []
+            for k in range(n):
+                if nsteps[k]:
+                    t[k] += int(nsteps[k])
+                    if events[k] is not None and events[k] == t[k]:
+                        acting.append((k, t[k]))
+                elif stage[k] == "final":
+                    acting.append((k, last[k] + 1))
+            if not acting:
+                if all(st == "done" for st in stage):
+                    break
+                continue
+            due = {}
+            for k, tk in acting:
+                kind = pms[k].stop_reduction_due(tk)
+                if kind is not None:
+                    due.setdefault(kind, []).append(k)
+            for kind, ks in due.items():
+                sel = np.zeros(n, dtype=np.uint8)
+                sel[ks] = 1
+                rows = batch.reduce(kind, sel)
+                for k in ks:
+                    models[k].lattice.prefetched[kind] = rows[k]
+            for k, tk in acting:
+                stop = pms[k].next(models[k], tk)
+                models[k].lattice.prefetched.clear()
+                if stage[k] == "final" or stop:
+                    stage[k] = "done"
+            if all(st == "done" for st in stage):
+                break
+    finally:
+        batch.close()
+    return models
+
+
 def simulate(problem_or_model, q=None, *, time=None, process_method=None, should_process=True,
              initialization_strategy=None, t_end=1.0, collision_model=SRT, storage="f64"):
     """Both entry points of the reference:

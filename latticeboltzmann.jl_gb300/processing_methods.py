@@ -48,6 +48,7 @@ def _sqrt(a):
 # ---------------------------------------------------------------------------------------
 class StopCriteria:
     active = True
+    reduce_kind = None  # the device reduction should_stop consumes (batched by simulate_batch)
 
     def should_stop(self, model) -> bool:
         return False
@@ -59,6 +60,7 @@ class NoStoppingCriteria(StopCriteria):
 
 class MeanVelocityStoppingCriteria(StopCriteria):
     """stopping_criteria.jl:20-72: stop when |ū_x / ū_x,old - 1| < tolerance, or on NaN."""
+    reduce_kind = N.REDUCE_MEAN_VELOCITY
 
     def __init__(self, old_mean_velocity, tolerance, problem):
         self.old_mean_velocity = float(old_mean_velocity)
@@ -80,6 +82,7 @@ class MeanVelocityStoppingCriteria(StopCriteria):
 class VelocityConvergenceStoppingCriteria(StopCriteria):
     """stopping_criteria.jl:74-132: √Σ|u - u_old|² / Σ|u_old|² < tolerance; the previous
     velocity field is kept on the device."""
+    reduce_kind = N.REDUCE_VELOCITY_CONVERGENCE
 
     def __init__(self, tolerance, problem):
         self.tolerance = float(tolerance)
@@ -138,6 +141,10 @@ class ProcessingMethodBase:
         """Smallest t >= t_from at which next() may act, or None."""
         return None
 
+    def stop_reduction_due(self, t: int):
+        """The device reduction kind next(model, t) will ask its stop criterion for, or None."""
+        return None
+
 
 class NoProcessing(ProcessingMethodBase):
     """A processing method that records nothing and never stops (pure stepping)."""
@@ -180,6 +187,9 @@ class TrackHydrodynamicErrors(ProcessingMethodBase):
     def next_event(self, t_from):
         return _events(t_from, self.should_process, self.stop_criteria.active, self.n_steps)
 
+    def stop_reduction_due(self, t):
+        return self.stop_criteria.reduce_kind if t % 100 == 0 else None
+
     def next(self, model, t):
         should_stop = False
         if t % 100 == 0 and self.stop_criteria.should_stop(model):
@@ -214,6 +224,9 @@ class CompareWithAnalyticalSolution(ProcessingMethodBase):
 
     def next_event(self, t_from):
         return _events(t_from, self.should_process, self.stop_criteria.active, self.n_steps)
+
+    def stop_reduction_due(self, t):
+        return self.stop_criteria.reduce_kind if t % 100 == 0 else None
 
     def next(self, model, t):
         if t % 100 == 0 and self.stop_criteria.should_stop(model):

@@ -120,3 +120,98 @@ def run_tgv_study(instances=None, storage="df64dev", sequential=True, torch=None
     for m in models:
         m.close()
     return res
+
+
+# ---------------------------------------------------------------------------------------
+# The TRT relaxation-time sweep of examples/notebooks/trt_magic_parameter.ipynb
+# ---------------------------------------------------------------------------------------
+def trt_sweep_points(taus_s, taus_a=None):
+    """All (τ_s, τ_a) pairs of the notebook's `for τ_s in τ_s_range, τ_a in τ_a_range` loop."""
+    taus_a = taus_s if taus_a is None else taus_a
+    return [(float(ts), float(ta)) for ts in taus_s for ta in taus_a]
+
+
+def julia_range(start, stop, step):
+    """Julia's range(start, stop=stop, step=step) of decimal literals: the element k is the double
+    nearest start + k·step taken exactly (what Julia's twice-precision ranges give for such
+    literals, e.g. 0.61 rather than 0.51 + 0.1), k = 0 .. floor((stop - start) / step)."""
+    from decimal import Decimal
+    a, b, h = Decimal(repr(start)), Decimal(repr(stop)), Decimal(repr(step))
+    n = int((b - a) // h) + 1
+    return [float(a + k * h) for k in range(n)]
+
+
+def build_trt_sweep_models(points, scale=1, quadrature="D2Q9", storage="f64"):
+    """One model per point as `solve(problem, q, τ_s, τ_a)` of the notebook builds it:
+    PoiseuilleFlow(ν, scale) with ν = (τ_s - 1/2) c_s², t_end = 100, TRT(τ_s, τ_a) with the
+    problem's lattice force, TrackHydrodynamicErrors(problem, false, n_steps,
+    VelocityConvergenceStoppingCriteria(1e-7, problem)), zero-velocity start.  Returns the
+    models and their time ranges 0:n_steps."""
+    from .collision_models import TRT
+    from .initial_conditions import ZeroVelocityInitialCondition
+    from .problems import PoiseuilleFlow
+    from .processing_methods import TrackHydrodynamicErrors, VelocityConvergenceStoppingCriteria
+    q = Quadratures[quadrature]
+    models, times = [], []
+    for ts, ta in points:
+        problem = PoiseuilleFlow((ts - 0.5) / q.speed_of_sound_squared, scale)
+        n_steps = int(round(100.0 / problem.delta_t()))
+        pm = TrackHydrodynamicErrors(problem, False, n_steps, VelocityConvergenceStoppingCriteria(1e-7, problem))
+        models.append(LatticeBoltzmannModel(problem, q, collision_model=TRT.fields(ts, ta, "problem"),
+                                            initialization_strategy=ZeroVelocityInitialCondition(),
+                                            process_method=pm, storage=storage))
+        times.append(range(0, n_steps + 1))
+    return models, times
+
+
+def run_trt_sweep(points, scale=1, storage="f64", batched=True, sequential_points=None, torch=None):
+    """The sweep batched (simulate_batch over all points) and, for `sequential_points` (a
+    subset, or all), one simulate after another.  Both arms build their models first and time
+    the time loops alone (wall clock, synchronised).  Returns rows, timings and runs per second."""
+    from .model import simulate_batch, simulate_model
+    if torch is None:
+        import torch
+    res = {"points": len(points), "scale": scale, "storage": storage}
+    rows = {}
+    if batched:
+        t0 = time.perf_counter()
+        models, times = build_trt_sweep_models(points, scale, storage=storage)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        simulate_batch(models, times)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        res["batched_setup_s"] = t1 - t0
+        res["batched_s"] = t2 - t1
+        res["batched_runs_per_s"] = len(points) / (t2 - t1)
+        res["batched_steps"] = int(sum(m.processing_method.df[-1].timestep for m in models))
+        for p, m in zip(points, models):
+            rows[p] = m.processing_method.df[-1]
+            m.close()
+    if sequential_points:
+        t0 = time.perf_counter()
+        models, times = build_trt_sweep_models(sequential_points, scale, storage=storage)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for m, tm in zip(models, times):
+            simulate_model(m, tm)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        res["sequential_points"] = len(sequential_points)
+        res["sequential_setup_s"] = t1 - t0
+        res["sequential_s"] = t2 - t1
+        res["sequential_runs_per_s"] = len(sequential_points) / (t2 - t1)
+        diffs = []
+        for p, m in zip(sequential_points, models):
+            r = m.processing_method.df[-1]
+            if p in rows:
+                b = rows[p]
+                diffs.append(max(abs(x - y) / max(abs(y), 1e-300) for x, y in zip(b, r)
+                                 if math.isfinite(x) and math.isfinite(y)))
+            m.close()
+        if diffs:
+            res["max_rel_diff_batched_vs_sequential"] = float(max(diffs))
+        if batched:
+            res["speedup_vs_sequential"] = res["batched_runs_per_s"] / res["sequential_runs_per_s"]
+    res["rows"] = rows
+    return res

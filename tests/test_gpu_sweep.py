@@ -1,0 +1,89 @@
+"""Batched time loops (simulate_batch over a DeviceBatch with batched stop-criterion
+reductions): the TRT relaxation-time sweep of examples/notebooks/trt_magic_parameter.ipynb."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gpu_cases import wave_field
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROWS = json.load(open(os.path.join(HERE, "golden", "trt_magic_parameter_rows.json")))["rows"]
+
+
+def test_batched_sweep_reproduces_the_notebook_rows(lbm_gpu):
+    """All 21 printed rows of the notebook, as ONE batch: error_u and error_p to the printed digits."""
+    lbm = lbm_gpu
+    points = [(r["tau_s"], r["tau_a"]) for r in ROWS]
+    models, times = lbm.build_trt_sweep_models(points, scale=1)
+    lbm.simulate_batch(models, times)
+    for r, m in zip(ROWS, models):
+        last = m.processing_method.df[-1]
+        assert last.error_u == pytest.approx(r["error_u"], rel=6e-6), r
+        assert last.error_p == pytest.approx(r["error_p"], rel=6e-6), r
+        m.close()
+
+
+def test_batched_sweep_equals_sequential(lbm_gpu):
+    """Runs that stop early, run to n_steps or blow up: every row field of every run is the same
+    batched and one after another (same kernels, same reduction order)."""
+    lbm = lbm_gpu
+    points = lbm.trt_sweep_points([0.51, 0.8, 1.7, 6.0], [0.51, 0.6, 1.3, 9.0])
+    res = {}
+    for mode in ("batched", "sequential"):
+        models, times = lbm.build_trt_sweep_models(points, scale=2)
+        if mode == "batched":
+            lbm.simulate_batch(models, times)
+        else:
+            for m, tm in zip(models, times):
+                lbm.simulate_model(m, tm)
+        res[mode] = [list(m.processing_method.df) for m in models]
+        for m in models:
+            m.close()
+    for a, b in zip(res["batched"], res["sequential"]):
+        assert len(a) == len(b)
+        for ra, rb in zip(a, b):
+            np.testing.assert_array_equal(np.array(ra, dtype=float), np.array(rb, dtype=float))
+
+
+def _lattices(lbm, storage):
+    out = []
+    for qname, nx, ny, seed in (("D2Q9", 40, 24, 1), ("D2Q13", 33, 17, 2), ("D2Q9", 5, 3, 3)):
+        q = lbm.Quadratures[qname]
+        f0 = wave_field(q, nx, ny, seed=seed, amp=0.01)
+        cm = lbm.TRT.fields(0.8, 1.1)
+        m = lbm.LatticeBoltzmannModel.from_parts(q, f0, cm, storage=storage)
+        out.append(m)
+    return out
+
+
+@pytest.mark.parametrize("storage", ["f64", "df64dev", "f32dev"])
+def test_batch_reduce_matches_single_lattice_reduce(lbm_gpu, storage):
+    lbm = lbm_gpu
+    N = lbm._native
+    A, B = _lattices(lbm, storage), _lattices(lbm, storage)
+    batch = lbm.DeviceBatch([m.lattice for m in A])
+    batch.step(np.array([7, 3, 0], dtype=np.int64))
+    for m, k in zip(B, (7, 3, 0)):
+        m.lattice.step(k, 0, 0.0)
+    for kind in (N.REDUCE_MEAN_VELOCITY, N.REDUCE_CONSERVED):
+        rows = batch.reduce(kind)
+        for k, m in enumerate(B):
+            np.testing.assert_array_equal(rows[k], m.lattice.reduce(kind)[: rows.shape[1]])
+    # velocity convergence updates the previous-velocity planes of the selected members only
+    sel = np.array([1, 0, 1], dtype=np.uint8)
+    for _ in range(2):
+        rows = batch.reduce(N.REDUCE_VELOCITY_CONVERGENCE, sel)
+        for k, m in enumerate(B):
+            if sel[k]:
+                np.testing.assert_array_equal(rows[k], m.lattice.reduce(N.REDUCE_VELOCITY_CONVERGENCE))
+            else:
+                assert not rows[k].any()
+    np.testing.assert_array_equal(batch.reduce(N.REDUCE_VELOCITY_CONVERGENCE)[1],
+                                  B[1].lattice.reduce(N.REDUCE_VELOCITY_CONVERGENCE))
+    batch.close()
+    for m in A + B:
+        m.close()
