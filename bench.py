@@ -239,6 +239,23 @@ def bench_batched(torch, lbm):
     return res
 
 
+def bench_trt_sweep(torch, lbm, every=40):
+    """The TRT relaxation-time sweep of trt_magic_parameter.ipynb (cell 2's grid τ_s, τ_a in
+    0.51:0.1:10.0, 9025 Poiseuille runs of PoiseuilleFlow(ν, 1), TRT with force, velocity
+    convergence stop at 1e-7, t_end = 100): all runs batched, and every `every`-th run one after
+    another for the sequential rate; rows of the common runs must agree bitwise."""
+    taus = lbm.julia_range(0.51, 10.0, 0.1)
+    pts = lbm.trt_sweep_points(taus)
+    res = lbm.run_trt_sweep(pts, scale=1, sequential_points=pts[::every], torch=torch)
+    rows = res.pop("rows")
+    res["workload"] = ("TRT (tau_s, tau_a) sweep of trt_magic_parameter.ipynb: 95 x 95 = 9025 D2Q9 Poiseuille "
+                       "runs (3 x 5 nodes, force, bounce-back, velocity-convergence stop), FP64; sequential "
+                       f"rate from every {every}th run")
+    best = min(rows.items(), key=lambda kv: kv[1].error_u if math.isfinite(kv[1].error_u) else math.inf)
+    res["best_point"] = {"tau_s": best[0][0], "tau_a": best[0][1], "error_u": best[1].error_u}
+    return res
+
+
 def bench_adjoint(torch, lbm, n=512, steps=4000):
     q = lbm.D2Q9()
     tau_s = 0.8
@@ -401,7 +418,8 @@ def main():
                          "error_after_steps": args.warmup + args.steps}
     if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
         extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
-                            "batched": bench_batched(torch, lbm), "adjoint": bench_adjoint(torch, lbm)}
+                            "batched": bench_batched(torch, lbm), "trt_sweep": bench_trt_sweep(torch, lbm),
+                            "adjoint": bench_adjoint(torch, lbm)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(tau_s)
