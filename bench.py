@@ -343,9 +343,9 @@ def main():
     ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev"])
     ap.add_argument("--profile", action="store_true",
                     help="time only the device loop of the chosen storage (for profiler runs)")
-    ap.add_argument("--case", default="poiseuille", choices=["poiseuille", "mrt_d2q37"],
-                    help="with --profile: the lattice whose device loop is timed (D2Q9 TRT Poiseuille "
-                         "4096^2, or D2Q37 regularised MRT shear wave 2048^2)")
+    ap.add_argument("--case", default="poiseuille", choices=["poiseuille", "mrt_d2q37", "trt_sweep", "adjoint"],
+                    help="with --profile: the workload run (D2Q9 TRT Poiseuille 4096^2, D2Q37 regularised MRT "
+                         "shear wave 2048^2, the batched TRT sweep, or the D2Q9 TRT 512^2 adjoint)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other configurations (Taylor-Green 64^2, D2Q37 MRT, batched study, adjoint)")
     args = ap.parse_args()
@@ -375,6 +375,15 @@ def main():
         m.close()
         print(json.dumps({"case": "mrt_d2q37", "storage": args.storage, "mlups": n * n * args.steps / sec / 1e6,
                           "launches": launches}))
+        return 0
+    if args.profile and args.case == "trt_sweep":  # 95 x 95 grid, every 8th point: 1129 runs
+        pts = lbm.trt_sweep_points(lbm.julia_range(0.51, 10.0, 0.1))[::8]
+        res = lbm.run_trt_sweep(pts, scale=1, torch=torch)
+        res.pop("rows")
+        print(json.dumps({"case": "trt_sweep", **res}))
+        return 0
+    if args.profile and args.case == "adjoint":
+        print(json.dumps({"case": "adjoint", **bench_adjoint(torch, lbm, steps=args.steps)}))
         return 0
 
     problem, model, f0 = build_model(lbm, args.storage, tau_s)

@@ -127,15 +127,19 @@ __global__ void __launch_bounds__(kAdjThreads) adj_loss_kernel(StepParams<typena
 // One reverse step: λ_t = J_C(A_t)^T S^T λ_{t+1}.  A_t is pulled from B_{t-1} (pull = true) or
 // read locally (A_0).  Parameter sensitivities are added to this block's slots.
 template <class L, class S, int COLL>
-__global__ void __launch_bounds__(kAdjThreads) adj_step_kernel(StepParams<typename S::C> p, AdjArgs a,
+__global__ void __launch_bounds__(kAdjThreads, (S::DEV && L::Q <= 9) ? 4 : 1) adj_step_kernel(StepParams<typename S::C> p, AdjArgs a,
                                                                const typename S::T* __restrict__ src, int pull,
                                                                const typename S::T* __restrict__ lam_next,
                                                                typename S::T* __restrict__ lam_out,
                                                                double* __restrict__ slots) {
   using CT = typename S::C;
-  double acc[kAdjParams] = {0, 0, 0, 0, 0};
+  // per-thread sums in the compute type (a thread owns about two nodes), widened to FP64 once
+  // for the block's fixed-order FP64 sum: no FP64 instruction per node
+  CT tacc[kAdjParams] = {0, 0, 0, 0, 0};
   const CT om_s = COLL == LBM_TRT ? p.inv_ts : p.om_b;
   const CT om_a = COLL == LBM_TRT ? p.inv_ta : p.om_b;
+  const CT Fx = (CT)a.Fx, Fy = (CT)a.Fy, shift = (CT)a.shift;
+  const CT sFx = (CT)(a.shift * a.Fx), sFy = (CT)(a.shift * a.Fy);
   for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
        node += (long long)gridDim.x * kAdjThreads) {
     const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_step_kernel(StepParams<typena
     const CT rho = S::DEV ? (CT)1 + s : s;
     const CT drho = s;
     const CT ux = jx / rho, uy = jy / rho;
-    const CT upx = ux + (CT)a.shift * (CT)a.Fx, upy = uy + (CT)a.shift * (CT)a.Fy;
+    const CT upx = ux + sFx, upy = uy + sFy;
     CT feq[L::Q], dfx[L::Q], dfy[L::Q];
     adj_equilibrium<L, S>(p, rho, drho, upx, upy, feq, dfx, dfy);
     // ν = N μ and M μ per opposite pair
@@ -177,8 +181,8 @@ __global__ void __launch_bounds__(kAdjThreads) adj_step_kernel(StepParams<typena
       nu[i] = om_s * ms + om_a * ma;
       Mmu[i] = ((CT)1 - om_s) * ms + ((CT)1 - om_a) * ma;
       const CT fneq = f[i] - feq[i];  // deviation storage: g - geq
-      acc[0] -= (double)(ms * fneq);
-      acc[1] -= (double)(ma * fneq);
+      tacc[0] -= ms * fneq;
+      tacc[1] -= ma * fneq;
     }
     CT Grho = 0, Gx = 0, Gy = 0;
 #pragma unroll
@@ -189,15 +193,18 @@ __global__ void __launch_bounds__(kAdjThreads) adj_step_kernel(StepParams<typena
       Gy += nu[i] * dfy[i];
     }
     Grho = Grho / rho;
-    acc[2] += (double)Gx * a.Fx + (double)Gy * a.Fy;
-    acc[3] += (double)a.shift * (double)Gx;
-    acc[4] += (double)a.shift * (double)Gy;
+    tacc[2] += Gx * Fx + Gy * Fy;
+    tacc[3] += shift * Gx;
+    tacc[4] += shift * Gy;
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
       const CT l = Mmu[i] + Grho + (Gx * ((CT)L::cx(i) - ux) + Gy * ((CT)L::cy(i) - uy)) / rho;
       lam_out[(size_t)i * p.n + node] = (typename S::T)l;
     }
   }
+  double acc[kAdjParams];
+#pragma unroll
+  for (int k = 0; k < kAdjParams; ++k) acc[k] = (double)tacc[k];
   adj_block_add<kAdjParams>(acc, slots);
 }
 

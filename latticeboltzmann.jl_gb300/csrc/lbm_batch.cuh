@@ -61,7 +61,9 @@ __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>&
 
 // One global step t over the first `nactive` members of one velocity set (members of other sets
 // run in their own launch of the same step).  A block covers kBlockX consecutive nodes (x
-// fastest) of one member, so lattices of a few nodes use a few threads, not a row of blocks.
+// fastest) of one member: a lattice of a few nodes takes one block, so the launch keeps one
+// block per small member in flight (packing several small members into one block leaves fewer
+// warps to hide the latency of a step that is pure latency at this size; measured slower).
 template <class L, class S, int COLL>
 __global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchStatic<typename S::C>* __restrict__ statics,
                                                              const BatchDyn* __restrict__ dyn, int nactive,
