@@ -256,6 +256,28 @@ def bench_trt_sweep(torch, lbm, every=40):
     return res
 
 
+def bench_init(torch, lbm, n=2048):
+    """Model construction with the Taylor-Green equilibrium + off-equilibrium initial condition:
+    the state built on the device from the macroscopic planes, against the host build of all Q
+    planes and their upload (the reference's initialize loop, vectorised)."""
+    q = lbm.D2Q9()
+    problem = lbm.TaylorGreenVortex(0.1, 1, n, n, static=False)
+    st = lbm.AnalyticalEquilibriumAndOffEquilibrium()
+    out = {"workload": f"LatticeBoltzmannModel(TaylorGreenVortex {n}x{n}, D2Q9, equilibrium + off-equilibrium)"}
+    f = {}
+    for name, dev in (("device_s", True), ("host_s", False)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m = lbm.LatticeBoltzmannModel(problem, q, initialization_strategy=st, device_init=dev)
+        torch.cuda.synchronize()
+        out[name] = time.perf_counter() - t0
+        f[name] = m.f_stream
+        m.close()
+    out["speedup"] = out["host_s"] / out["device_s"]
+    out["max_abs_diff"] = float(np.max(np.abs(f["device_s"] - f["host_s"])))
+    return out
+
+
 def bench_adjoint(torch, lbm, n=512, steps=4000):
     q = lbm.D2Q9()
     tau_s = 0.8
@@ -428,6 +450,7 @@ def main():
     if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
         extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
                             "batched": bench_batched(torch, lbm), "trt_sweep": bench_trt_sweep(torch, lbm),
+                            "init": bench_init(torch, lbm),
                             "adjoint": bench_adjoint(torch, lbm)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:

@@ -139,6 +139,20 @@ int32_t lbm_download(lbm_ctx* ctx, double* f_host);
 int32_t lbm_upload_device(lbm_ctx* ctx, const double* f_device);
 int32_t lbm_download_device(lbm_ctx* ctx, double* f_device);
 
+/* The initial state computed on the device from macroscopic planes (host arrays of nx*ny
+ * doubles, Julia layout), instead of uploading Q planes built on the host by
+ * `initialize(strategy, q, problem)` (initial_conditions.jl:7-22):
+ *   f_i = equilibrium(q, ρ, u, T)_i   the Hermite expansion of hermite.jl:10-33
+ *       + stress_coef [· ρ when stress_times_rho] · w_i · H_2(c_i) : S,  S = [sxx sxy; sxy syy]
+ * which covers AnalyticalEquilibrium (analytical_equilibrium.jl), AnalyticalEquilibriumAndOff-
+ * Equilibrium (analytical_offequilibrium.jl:10-87, both forms), ConstantDensity and
+ * AnalyticalVelocityAndStress, and ZeroVelocityInitialCondition (everything NULL: f = w).
+ * rho / T NULL mean 1, ux / uy NULL mean 0; sxx, sxy, syy are all given or all NULL.
+ * The state becomes f_stream, as after lbm_upload. */
+int32_t lbm_initialize_fields(lbm_ctx* ctx, const double* rho, const double* ux, const double* uy, const double* T,
+                              const double* sxx, const double* sxy, const double* syy, double stress_coef,
+                              int32_t stress_times_rho);
+
 /* `nsteps` iterations of the reference loop body for t = t0, ..., t0 + nsteps - 1:
  * collide!(time = t*dt) -> stream! -> apply!(bcs), as simulate(model, time) does
  * (src/lattice_boltzmann_model.jl:64-67).  Asynchronous on the context's stream. */

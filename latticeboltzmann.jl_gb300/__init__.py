@@ -27,7 +27,7 @@ from .problems import (FluidFlowProblem, TaylorGreenVortex, TGV, PoiseuilleFlow,
                        problem_range, delta_t, delta_x, viscosity, lattice_viscosity, has_external_force,
                        boundary_conditions, lattice_velocity, lattice_density, lattice_pressure, lattice_temperature,
                        lattice_force_field, analytic_fields, decay_time, node_grid)
-from .initial_conditions import (InitializationStrategy, ZeroVelocityInitialCondition, AnalyticalEquilibrium,
+from .initial_conditions import (InitializationStrategy, ZeroVelocityInitialCondition, AnalyticalEquilibrium, initial_fields,
                                  AnalyticalEquilibriumAndOffEquilibrium, ConstantDensity, AnalyticalVelocityAndStress,
                                  AnalyticalVelocity, IterativeInitializationMeiEtAl, IterativeInitialization,
                                  initialize)

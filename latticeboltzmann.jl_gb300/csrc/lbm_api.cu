@@ -645,6 +645,48 @@ static int upload_impl(lbm_ctx* c, const double* f, cudaMemcpyKind kind) {
   return LBM_OK;
 }
 
+int32_t lbm_initialize_fields(lbm_ctx* c, const double* rho, const double* ux, const double* uy, const double* T,
+                              const double* sxx, const double* sxy, const double* syy, double stress_coef,
+                              int32_t stress_times_rho) {
+  if (!c) return LBM_ERR_INVALID;
+  const bool any_s = sxx || sxy || syy, all_s = sxx && sxy && syy;
+  if (any_s && !all_s) return fail(c, LBM_ERR_INVALID, "the stress tensor needs sxx, sxy and syy");
+  cudaSetDevice(c->device);
+  const double* host[7] = {rho, ux, uy, T, sxx, sxy, syy};
+  int nplanes = 0;
+  for (const double* h : host) nplanes += h ? 1 : 0;
+  double* d = nullptr;
+  if (nplanes > 0) {
+    cudaError_t e = cudaMalloc((void**)&d, (size_t)c->n * nplanes * sizeof(double));
+    if (e != cudaSuccess) return fail(c, LBM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  const double* dev[7] = {};
+  int k = 0;
+  for (int j = 0; j < 7; ++j) {
+    if (!host[j]) continue;
+    double* plane = d + (size_t)k++ * c->n;
+    cudaError_t e = cudaMemcpyAsync(plane, host[j], (size_t)c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      return cuda_fail(c, e, "cudaMemcpyAsync");
+    }
+    dev[j] = plane;
+  }
+  InitFields in{dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], dev[6], stress_coef, stress_times_rho ? 1 : 0};
+  OpArgs a = base_args(c, OP_INIT_FIELDS);
+  a.init = &in;
+  a.dst = c->buf[0];
+  int rc = run(c, a);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaFree(d);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(c, e, "initialize");
+  c->cur = 0;
+  c->phase = POST_STREAM;
+  c->have_state = true;
+  return LBM_OK;
+}
+
 int32_t lbm_upload(lbm_ctx* c, const double* f) { return upload_impl(c, f, cudaMemcpyHostToDevice); }
 int32_t lbm_upload_device(lbm_ctx* c, const double* f) { return upload_impl(c, f, cudaMemcpyDeviceToDevice); }
 

@@ -16,7 +16,8 @@ enum Op {
   OP_MACRO = 6,      // ρ, u planes
   OP_WIDEN = 7,      // observed populations -> FP64 planes
   OP_NARROW = 8,     // FP64 planes -> storage
-  OP_NODE_DENSITY = 9  // density of node (node_x, node_y)
+  OP_NODE_DENSITY = 9,  // density of node (node_x, node_y)
+  OP_INIT_FIELDS = 10   // initial populations from macroscopic planes
 };
 
 struct OpArgs {
@@ -33,6 +34,7 @@ struct OpArgs {
   int nblocks = 0;
   double* out = nullptr;
   int node_x = 0, node_y = 0;
+  const InitFields* init = nullptr;
   cudaStream_t stream = 0;
 };
 
@@ -119,6 +121,9 @@ inline cudaError_t run_op_s(const OpArgs& a, const StepParams<typename S::C>& p)
     case OP_NARROW:
       narrow_kernel<L, S><<<g, kBlockX, 0, a.stream>>>(p, *a.red, static_cast<const double*>(a.src),
                                                        static_cast<typename S::T*>(a.dst));
+      break;
+    case OP_INIT_FIELDS:
+      init_fields_kernel<L, S><<<g, kBlockX, 0, a.stream>>>(p, *a.red, *a.init, static_cast<typename S::T*>(a.dst));
       break;
     case OP_NODE_DENSITY:
       if (a.pull)

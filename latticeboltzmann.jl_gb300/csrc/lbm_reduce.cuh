@@ -253,6 +253,120 @@ __global__ void __launch_bounds__(kBlockX) narrow_kernel(StepParams<typename S::
   }
 }
 
+// Macroscopic planes of the initial conditions (n doubles each, Julia layout; NULL = default).
+struct InitFields {
+  const double *rho, *ux, *uy, *T;  // defaults 1, 0, 0, 1
+  const double *sxx, *sxy, *syy;    // symmetric stress-term tensor S (all NULL: no stress term)
+  double coef;                      // stress-term coefficient
+  int times_rho;                    // the stress term is also multiplied by ρ
+};
+
+// Initial populations from macroscopic fields, in FP64 whatever the storage
+// (src/initial_conditions/*.jl):
+//   f_i = w_i (ρ + Σ_{n=1..N} a_eq^(n)(ρ, u, T) : H_n(c_i) / (n! c_s^{2n}))
+// the Hermite equilibrium `equilibrium(q, ρ, u, T)` of hermite.jl:10-33 (N = order(q) ÷ 2,
+// a_eq^(n) of hermite.jl:37-77 including its repeated δ(b,d) / δ(a,d) terms at n = 4, H_n of
+// hermite_polynomials.jl:47-82 with c_s² in the isotropic terms; tensor sums in column-major
+// order), plus the stress term coef [ρ] w_i H_2(c_i) : S of analytical_offequilibrium.jl:10-87
+// and analytical_velocity_stress.jl.
+template <class L, class S>
+__global__ void __launch_bounds__(kBlockX) init_fields_kernel(StepParams<typename S::C> p, ReduceArgs r,
+                                                              InitFields in, typename S::T* __restrict__ dst) {
+  const int x = blockIdx.x * kBlockX + threadIdx.x;
+  if (x >= p.nx) return;
+  const double css = 1.0 / r.cs;  // c_s²
+  for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
+    const size_t k = (size_t)y * p.nx + x;
+    const double rho = in.rho ? in.rho[k] : 1.0;
+    const double u[2] = {in.ux ? in.ux[k] : 0.0, in.uy ? in.uy[k] : 0.0};
+    const double T = in.T ? in.T[k] : 1.0;
+    const double lam = css * (T - 1.0), lam2 = (css * css) * ((T - 1.0) * (T - 1.0));
+    auto d = [](int a, int b) { return a == b ? 1.0 : 0.0; };
+    double a1[2], a2[2][2], a3[2][2][2], a4[2][2][2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a) a1[a] = rho * u[a];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) a2[a][b] = rho * (a == b ? u[a] * u[b] + lam : u[a] * u[b]);
+    if constexpr (L::HN >= 3) {
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+          for (int c = 0; c < 2; ++c)
+            a3[a][b][c] = rho * (u[a] * u[b] * u[c] + lam * ((u[a] * d(b, c) + u[b] * d(a, c)) + u[c] * d(a, b)));
+    }
+    if constexpr (L::HN >= 4) {
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+          for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int e = 0; e < 2; ++e)
+              a4[a][b][c][e] = rho * (u[a] * u[b] * u[c] * u[e] +
+                                      lam * (u[a] * u[b] * d(c, e) + u[a] * u[c] * d(b, e) + u[a] * u[e] * d(b, e) +
+                                             u[b] * u[c] * d(a, e) + u[b] * u[e] * d(a, e) + u[c] * u[e] * d(a, b)) +
+                                      lam2 * (d(a, b) * d(c, e) + d(a, c) * d(b, e) + d(a, e) * d(b, c)));
+    }
+    static_for<0, L::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const double cv[2] = {(double)L::cx(i), (double)L::cy(i)};
+      double acc = 0.0 + a1[0] * cv[0];
+      acc = acc + a1[1] * cv[1];
+      double s = acc / css;
+      if constexpr (L::HN >= 2) {
+        acc = 0.0;
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+          for (int a = 0; a < 2; ++a) acc = acc + a2[a][b] * (cv[b] * cv[a] - css * d(a, b));
+        s = s + acc / (2.0 * (css * css));
+      }
+      if constexpr (L::HN >= 3) {
+        acc = 0.0;
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+              acc = acc + a3[a][b][c] * (cv[c] * cv[b] * cv[a] -
+                                         css * (cv[a] * d(b, c) + cv[b] * d(a, c) + cv[c] * d(a, b)));
+        s = s + acc / (6.0 * (css * css * css));
+      }
+      if constexpr (L::HN >= 4) {
+        acc = 0.0;
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+          for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+              for (int a = 0; a < 2; ++a) {
+                const double H = cv[e] * cv[c] * cv[b] * cv[a] -
+                                 css * (cv[a] * cv[b] * d(c, e) + cv[a] * cv[c] * d(b, e) + cv[a] * cv[e] * d(b, c) +
+                                        cv[b] * cv[c] * d(a, e) + cv[b] * cv[e] * d(a, c) + cv[c] * cv[e] * d(a, b)) +
+                                 (css * css) * (d(a, b) * d(c, e) + d(a, c) * d(b, e) + d(a, e) * d(b, c));
+                acc = acc + a4[a][b][c][e] * H;
+              }
+        s = s + acc / (24.0 * (css * css * css * css));
+      }
+      double f = r.w[i] * (rho + s);
+      if (in.sxx) {
+        const double HS = (cv[0] * cv[0] - css) * in.sxx[k] + (cv[1] * cv[0]) * in.sxy[k] +
+                          (cv[0] * cv[1]) * in.sxy[k] + (cv[1] * cv[1] - css) * in.syy[k];
+        f = f + (in.coef * (in.times_rho ? rho : 1.0)) * r.w[i] * HS;
+      }
+      S::st(dst + (size_t)i * p.n + k, (typename S::C)(S::DEV ? f - r.w[i] : f));
+    });
+  }
+}
+
 // Density of one node of the observed state (DensityConvergence, density_convergence.jl:6-17).
 template <class L, class S, bool PULL>
 __global__ void node_density_kernel(StepParams<typename S::C> p, ReduceArgs r, const typename S::T* __restrict__ src,

@@ -139,6 +139,22 @@ class DeviceLattice:
         f = _as_f64(f, self.shape)
         N.check(self.h, N.lib().lbm_upload(self.h, f.ctypes.data))
 
+    def initialize_fields(self, rho=None, ux=None, uy=None, T=None, S=None, coef=0.0, times_rho=False):
+        """lbm_initialize_fields: the initial state from macroscopic (NY, NX) planes, computed on
+        the device (None: ρ = 1, u = 0, T = 1, no stress term; S = (sxx, sxy, syy))."""
+        shp = (self.ny, self.nx)
+        keep = []
+
+        def ptr(a):
+            if a is None:
+                return None
+            a = _as_f64(np.broadcast_to(a, shp))
+            keep.append(a)
+            return a.ctypes.data_as(N._DP)
+        s = (None, None, None) if S is None else S
+        N.check(self.h, N.lib().lbm_initialize_fields(self.h, ptr(rho), ptr(ux), ptr(uy), ptr(T), ptr(s[0]),
+                                                       ptr(s[1]), ptr(s[2]), float(coef), 1 if times_rho else 0))
+
     def download(self, out=None):
         if out is not None and hasattr(out, "data_ptr"):
             fn = N.lib().lbm_download_device if out.is_cuda else N.lib().lbm_download

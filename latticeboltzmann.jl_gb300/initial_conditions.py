@@ -72,6 +72,41 @@ def _dot_sym(H, S):
     return acc
 
 
+def initial_fields(strategy, q, problem):
+    """The macroscopic planes from which `initialize` builds f, for the device-side build
+    (DeviceLattice.initialize_fields / lbm_initialize_fields): a dict of keyword arguments, or
+    None for a strategy that is not a closed-form field (the Mei iteration)."""
+    if isinstance(strategy, ZeroVelocityInitialCondition):
+        return {}
+    X, Y = node_grid(problem)
+    cs = q.speed_of_sound_squared
+
+    def sym(g):
+        return (g[0, 0] + g[0, 0], g[0, 1] + g[1, 0], g[1, 1] + g[1, 1])
+
+    if isinstance(strategy, (AnalyticalEquilibrium, AnalyticalEquilibriumAndOffEquilibrium)):
+        out = {"rho": problem.density(q, X, Y, 0.0), "T": problem.pressure(q, X, Y) / problem.density(q, X, Y)}
+        out["ux"], out["uy"] = lattice_velocity(q, problem, X, Y)
+        if isinstance(strategy, AnalyticalEquilibriumAndOffEquilibrium):
+            tau = cs * problem.lattice_viscosity()
+            if isinstance(problem, TGV):  # analytical_offequilibrium.jl:50-87
+                out["S"] = sym(problem.velocity_gradient(X, Y, 0.0))
+                out["coef"], out["times_rho"] = -(cs * (tau + 0.5)) / 2, True
+            else:  # analytical_offequilibrium.jl:10-49
+                out["S"] = sym(problem.u_max ** 2 * problem.velocity_gradient(X, Y, 0.0))
+                factor = problem.domain_size[0] * problem.domain_size[1]
+                out["coef"] = -factor * 0.5 * ((tau + 0.5) * cs)
+        return out
+    if isinstance(strategy, (ConstantDensity, AnalyticalVelocityAndStress)):
+        out = {}
+        out["ux"], out["uy"] = lattice_velocity(q, problem, X, Y)
+        if isinstance(strategy, AnalyticalVelocityAndStress):
+            out["S"] = sym(problem.u_max ** 2 * problem.velocity_gradient(X, Y, 0.0))
+            out["coef"] = -(cs * (cs * problem.lattice_viscosity() + 0.5)) / 2
+        return out
+    return None
+
+
 def initialize(strategy, q, problem, cm=None):
     X, Y = node_grid(problem)
     shape = X.shape

@@ -14,7 +14,7 @@ import numpy as np
 from . import _native as N
 from .collision_models import (IterativeInitializationCollisionModel, MRT, SRT, TRT, make_collision_model)
 from .device import DeviceLattice
-from .initial_conditions import default_strategy, initialize
+from .initial_conditions import default_strategy, initial_fields, initialize
 from .problems import DecayingShearFlow, PoiseuilleFlow, CouetteFlow, lattice_force_field, problem_range
 from .processing_methods import NoProcessing, ProcessIterativeInitialization, ProcessingMethod
 
@@ -44,7 +44,7 @@ class LatticeBoltzmannModel:
     FP16 deviation storage ("f32dev" / "f16dev")."""
 
     def __init__(self, problem, quadrature, collision_model=SRT, initialization_strategy=None,
-                 process_method=None, storage="f64", f0=None):
+                 process_method=None, storage="f64", f0=None, device_init=True):
         q = quadrature
         self.quadrature = q
         self.problem = problem
@@ -52,11 +52,19 @@ class LatticeBoltzmannModel:
         self.collision_model = make_collision_model(collision_model, q, problem)
         self.boundary_conditions = problem.boundary_conditions()
         self.processing_method = process_method if process_method is not None else NoProcessing(problem)
-        f = initialize(strategy, q, problem, collision_model) if f0 is None else f0
+        # closed-form initial conditions are built on the device from their macroscopic planes
+        # (lbm_initialize_fields); the rest, and explicit f0, are uploaded
+        fields = initial_fields(strategy, q, problem) if f0 is None and device_init else None
+        f = None
+        if fields is None:
+            f = initialize(strategy, q, problem, collision_model) if f0 is None else f0
         force = _force_descriptor(self.collision_model, q, problem)
         self.lattice = DeviceLattice(q, problem.NX, problem.NY, self.collision_model, self.boundary_conditions,
                                      force=force, storage=storage)
-        self.lattice.upload(f)
+        if fields is None:
+            self.lattice.upload(f)
+        else:
+            self.lattice.initialize_fields(**fields)
 
     @classmethod
     def from_parts(cls, quadrature, f0, collision_model, boundary_conditions=(), force=None, storage="f64",
