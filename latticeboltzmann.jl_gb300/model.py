@@ -149,6 +149,12 @@ def simulate_batch(models, times):
     pms = [m.processing_method for m in models]
     batch = DeviceBatch([m.lattice for m in models])
     batch.share_stream()
+    if all(_vectorisable(pm) for pm in pms):
+        try:
+            _simulate_batch_vectorised(models, pms, bounds, batch)
+        finally:
+            batch.close()
+        return models
     stage = ["loop"] * n  # loop -> final (the last next!) -> done
     try:
         while True:
@@ -199,6 +205,84 @@ def simulate_batch(models, times):
     finally:
         batch.close()
     return models
+
+
+def _vectorisable(pm):
+    from .processing_methods import (CompareWithAnalyticalSolution, MeanVelocityStoppingCriteria,
+                                     NoStoppingCriteria, TrackHydrodynamicErrors, VelocityConvergenceStoppingCriteria)
+    return (type(pm) in (TrackHydrodynamicErrors, CompareWithAnalyticalSolution) and not pm.should_process and
+            type(pm.stop_criteria) in (NoStoppingCriteria, MeanVelocityStoppingCriteria,
+                                       VelocityConvergenceStoppingCriteria))
+
+
+def _simulate_batch_vectorised(models, pms, bounds, batch):
+    """simulate_batch for TrackHydrodynamicErrors / CompareWithAnalyticalSolution without
+    per-step processing, with the members' bookkeeping in arrays: their events (every 100 steps
+    for a stop criterion, and n_steps) and their stop decisions are computed for all members at
+    once, and a member's own next!(model, t) is called only where it does more than decide not
+    to stop (a row is due, or it stops); a MeanVelocity criterion that does not stop keeps its
+    new mean as next! would (stopping_criteria.jl:20-72)."""
+    n = len(models)
+    t = np.array([b[0] for b in bounds], dtype=np.int64)
+    last = np.array([b[1] for b in bounds], dtype=np.int64)
+    nst = np.array([pm.n_steps for pm in pms], dtype=np.int64)
+    kind = np.array([-1 if pm.stop_criteria.reduce_kind is None else pm.stop_criteria.reduce_kind for pm in pms])
+    stop_on = kind >= 0
+    tol = np.array([getattr(pm.stop_criteria, "tolerance", 0.0) for pm in pms])
+    mean_old = np.array([getattr(pm.stop_criteria, "old_mean_velocity", 0.0) for pm in pms])
+    stage = np.zeros(n, dtype=np.int8)  # 0: time loop, 1: the final next!(model, last + 1), 2: done
+    big = np.iinfo(np.int64).max // 4
+    while True:
+        loop = stage == 0
+        ended = loop & (t > last)
+        stage[ended] = 1
+        loop &= ~ended
+        tf = t + 1
+        ev = np.where(stop_on, ((tf + 99) // 100) * 100, big)
+        ev = np.where(nst >= tf, np.minimum(ev, nst), ev)
+        steps = np.where(ev > last + 1, last - t + 1, np.maximum(1, ev - t))
+        steps = np.where(loop, steps, 0).astype(np.int64)
+        if steps.any():
+            batch.step(steps)
+        t = t + steps
+        act_loop = loop & (ev == t)
+        act_final = stage == 1
+        tact = np.where(act_final, last + 1, t)
+        acting = act_loop | act_final
+        due = acting & stop_on & (tact % 100 == 0)
+        stop = np.zeros(n, dtype=bool)
+        rows = {}
+        um = None
+        for kd in np.unique(kind[due]):
+            sel = due & (kind == kd)
+            r = batch.reduce(int(kd), sel.astype(np.uint8))
+            rows[int(kd)] = r
+            with np.errstate(divide="ignore", invalid="ignore"):
+                if kd == N.REDUCE_VELOCITY_CONVERGENCE:
+                    conv = np.sqrt(r[:, 0]) / r[:, 1]
+                    st = (conv < tol) | np.isnan(conv)
+                else:
+                    um = r[:, 0] / r[:, 1]
+                    conv = np.abs(um / mean_old - 1)
+                    st = (conv < tol) | np.isnan(um)
+            stop[sel] = st[sel]
+        call = acting & (stop | (tact == nst))
+        for k in np.flatnonzero(call):
+            lat = models[k].lattice
+            if due[k]:
+                lat.prefetched[int(kind[k])] = rows[int(kind[k])][k]
+            stop[k] = bool(pms[k].next(models[k], int(tact[k])))
+            lat.prefetched.clear()
+            if kind[k] == N.REDUCE_MEAN_VELOCITY:
+                mean_old[k] = pms[k].stop_criteria.old_mean_velocity
+        kept = due & ~call & (kind == N.REDUCE_MEAN_VELOCITY)
+        for k in np.flatnonzero(kept):
+            mean_old[k] = um[k]
+            pms[k].stop_criteria.old_mean_velocity = float(um[k])
+        stage[act_final] = 2
+        stage[act_loop & stop] = 2
+        if (stage == 2).all():
+            return
 
 
 def simulate(problem_or_model, q=None, *, time=None, process_method=None, should_process=True,

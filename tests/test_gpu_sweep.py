@@ -87,3 +87,67 @@ def test_batch_reduce_matches_single_lattice_reduce(lbm_gpu, storage):
     batch.close()
     for m in A + B:
         m.close()
+
+
+def _mixed_models(lbm):
+    """Runs with MeanVelocity stop criteria (the reference's defaults for Poiseuille and Couette),
+    TrackHydrodynamicErrors and CompareWithAnalyticalSolution, uneven sizes and run lengths."""
+    q = lbm.D2Q9()
+    models, times = [], []
+    for k, (nu, scale) in enumerate([(0.05, 1), (0.1, 2), (0.3, 1), (0.8, 2), (0.02, 1)]):
+        for kind in ("poiseuille", "couette"):
+            problem = (lbm.PoiseuilleFlow(nu, scale) if kind == "poiseuille" else lbm.CouetteFlow(nu, scale))
+            n_steps = int(round(5.0 / problem.delta_t()))
+            pm = (lbm.TrackHydrodynamicErrors(problem, False, n_steps) if k % 2 == 0
+                  else lbm.CompareWithAnalyticalSolution(problem, False, n_steps))
+            models.append(lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.TRT, process_method=pm,
+                                                    initialization_strategy=lbm.ZeroVelocityInitialCondition()))
+            times.append(range(0, n_steps + 1))
+    return models, times
+
+
+def test_batched_mean_velocity_and_compare_equal_sequential(lbm_gpu):
+    lbm = lbm_gpu
+    res = {}
+    for mode in ("batched", "sequential"):
+        models, times = _mixed_models(lbm)
+        if mode == "batched":
+            lbm.simulate_batch(models, times)
+        else:
+            for m, tm in zip(models, times):
+                lbm.simulate_model(m, tm)
+        res[mode] = [(list(m.processing_method.df), m.processing_method.stop_criteria.old_mean_velocity)
+                     for m in models]
+        for m in models:
+            m.close()
+    for (ra, oa), (rb, ob) in zip(res["batched"], res["sequential"]):
+        assert oa == ob
+        assert len(ra) == len(rb) and len(ra) >= 1
+        for a, b in zip(ra, rb):
+            np.testing.assert_array_equal(np.array(a, dtype=float), np.array(b, dtype=float))
+
+
+def test_batched_generic_path_every_step_processing(lbm_gpu):
+    """should_process = true (a row every step) takes the per-member path of simulate_batch."""
+    lbm = lbm_gpu
+    res = {}
+    for mode in ("batched", "sequential"):
+        q = lbm.D2Q9()
+        models = []
+        for nx in (16, 24, 8):
+            problem = lbm.TaylorGreenVortex(0.1, 1, nx, nx, static=False)
+            pm = lbm.TrackHydrodynamicErrors(problem, True, 60)
+            models.append(lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.SRT, process_method=pm))
+        times = [range(0, 40), range(0, 60), range(0, 25)]
+        if mode == "batched":
+            lbm.simulate_batch(models, times)
+        else:
+            for m, tm in zip(models, times):
+                lbm.simulate_model(m, tm)
+        res[mode] = [list(m.processing_method.df) for m in models]
+        for m in models:
+            m.close()
+    for a, b in zip(res["batched"], res["sequential"]):
+        assert len(a) == len(b)
+        for ra, rb in zip(a, b):
+            np.testing.assert_array_equal(np.array(ra, dtype=float), np.array(rb, dtype=float))
