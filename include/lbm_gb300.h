@@ -221,7 +221,8 @@ int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old); 
  * A convergence study or a parameter sweep is a set of independent lattices (one `simulate` per
  * point in the reference, e.g. examples/notebooks/taylor_green_vortex.ipynb cell 3 and
  * examples/notebooks/trt_magic_parameter.ipynb).  A batch groups existing contexts (same
- * storage, SRT or TRT, velocity sets D2Q4..D2Q17, no time-dependent force) and advances member k
+ * storage and collision model kind -- SRT, TRT or MRT --, any velocity set, FP64, float-float or
+ * FP32-deviation storage, no time-dependent force) and advances member k
  * by nsteps[k] steps with ONE graph launch: one kernel per global step, covering every member
  * still running.  Members keep their buffers; upload / download / reduce them as usual before
  * and after (their streams are ordered against the batch). */

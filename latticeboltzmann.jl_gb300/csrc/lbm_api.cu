@@ -969,8 +969,7 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
   for (int k = 0; k < count; ++k) {
     const lbm_ctx* c = members[k];
     if (!c || c->device != c0->device || c->storage != c0->storage || c->coll != c0->coll) return LBM_ERR_INVALID;
-    if (c->qid > LBM_D2Q17) return LBM_ERR_UNSUPPORTED;
-    if (c->coll != LBM_SRT && c->coll != LBM_TRT) return LBM_ERR_UNSUPPORTED;
+    if (c->coll == LBM_ITERATIVE_INIT) return LBM_ERR_UNSUPPORTED;
     if (c->storage == LBM_STORE_F16_DEV) return LBM_ERR_UNSUPPORTED;
     if (c->force_kind == LBM_FORCE_SHEAR) return LBM_ERR_UNSUPPORTED;  // time-dependent forces
   }

@@ -124,4 +124,86 @@ __global__ void batch_reduce_finish(const BatchDyn* __restrict__ dyn, int nmem, 
   out[(size_t)d.member * kRedMaxK + k] = s;
 }
 
+// ---- launchers, instantiated per velocity set in lbm_batch_q*.cu ----------------------------
+
+template <class L, class S>
+cudaError_t batch_step_s(int coll, const void* statics, const BatchDyn* dyn, int nactive, long long blocks,
+                         long long t, cudaStream_t s) {
+  const dim3 g((unsigned)blocks);
+  const auto* m = static_cast<const BatchStatic<typename S::C>*>(statics);
+  switch (coll) {
+    case LBM_SRT: batch_step_kernel<L, S, LBM_SRT><<<g, kBlockX, 0, s>>>(m, dyn, nactive, t); break;
+    case LBM_TRT: batch_step_kernel<L, S, LBM_TRT><<<g, kBlockX, 0, s>>>(m, dyn, nactive, t); break;
+    case LBM_MRT: batch_step_kernel<L, S, LBM_MRT><<<g, kBlockX, 0, s>>>(m, dyn, nactive, t); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// One global step t for the first `nactive` members (in launch order) of velocity set L.
+template <class L>
+cudaError_t batch_launch_set(int storage, int coll, const void* statics, const BatchDyn* dyn, int nactive,
+                             long long blocks, long long t, cudaStream_t s) {
+  if (blocks <= 0) return cudaSuccess;
+  switch (storage) {
+    case LBM_STORE_F64: return batch_step_s<L, F64>(coll, statics, dyn, nactive, blocks, t, s);
+    case LBM_STORE_DF64_DEV: return batch_step_s<L, DF64Dev>(coll, statics, dyn, nactive, blocks, t, s);
+    case LBM_STORE_F32_DEV: return batch_step_s<L, F32Dev>(coll, statics, dyn, nactive, blocks, t, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class L, class S>
+cudaError_t batch_reduce_s(int K, const void* statics, const ReduceArgs* args, const BatchDyn* dyn, int nmem,
+                           long long blocks, double* partial, long long part_base, double* out, cudaStream_t s) {
+  const auto* m = static_cast<const BatchStatic<typename S::C>*>(statics);
+  double* part = partial + (size_t)part_base * K;
+  const int fin_threads = 128, fin_blocks = (nmem * K + fin_threads - 1) / fin_threads;
+  switch (K) {
+    case 2:
+      batch_reduce_kernel<L, S, 2><<<(unsigned)blocks, kRedThreads, 0, s>>>(m, args, dyn, nmem, part);
+      batch_reduce_finish<2><<<fin_blocks, fin_threads, 0, s>>>(dyn, nmem, partial, part_base, out);
+      break;
+    case 3:
+      batch_reduce_kernel<L, S, 3><<<(unsigned)blocks, kRedThreads, 0, s>>>(m, args, dyn, nmem, part);
+      batch_reduce_finish<3><<<fin_blocks, fin_threads, 0, s>>>(dyn, nmem, partial, part_base, out);
+      break;
+    case 4:
+      batch_reduce_kernel<L, S, 4><<<(unsigned)blocks, kRedThreads, 0, s>>>(m, args, dyn, nmem, part);
+      batch_reduce_finish<4><<<fin_blocks, fin_threads, 0, s>>>(dyn, nmem, partial, part_base, out);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// Reductions of the `nmem` members (in launch order) of velocity set L: partial sums from block
+// part_base on, one row of kRedMaxK doubles per member (by static index) in `out`.
+template <class L>
+cudaError_t batch_reduce_set(int storage, int K, const void* statics, const ReduceArgs* args, const BatchDyn* dyn,
+                             int nmem, long long blocks, double* partial, long long part_base, double* out,
+                             cudaStream_t s) {
+  if (blocks <= 0 || nmem <= 0) return cudaSuccess;
+  switch (storage) {
+    case LBM_STORE_F64: return batch_reduce_s<L, F64>(K, statics, args, dyn, nmem, blocks, partial, part_base, out, s);
+    case LBM_STORE_DF64_DEV:
+      return batch_reduce_s<L, DF64Dev>(K, statics, args, dyn, nmem, blocks, partial, part_base, out, s);
+    case LBM_STORE_F32_DEV:
+      return batch_reduce_s<L, F32Dev>(K, statics, args, dyn, nmem, blocks, partial, part_base, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+#define LBM_BATCH_INSTANTIATE(NAME, LAT)                                                                         \
+  cudaError_t batch_launch_##NAME(int storage, int coll, const void* statics, const BatchDyn* dyn, int nactive, \
+                                  long long blocks, long long t, cudaStream_t s) {                              \
+    return batch_launch_set<LAT>(storage, coll, statics, dyn, nactive, blocks, t, s);                           \
+  }                                                                                                             \
+  cudaError_t batch_reduce_##NAME(int storage, int K, const void* statics, const ReduceArgs* args,              \
+                                  const BatchDyn* dyn, int nmem, long long blocks, double* partial,             \
+                                  long long part_base, double* out, cudaStream_t s) {                           \
+    return batch_reduce_set<LAT>(storage, K, statics, args, dyn, nmem, blocks, partial, part_base, out, s);     \
+  }
+
 }  // namespace lbm

@@ -1,0 +1,7 @@
+// Batched step and reduction kernels for the D2Q37 velocity set (own translation unit, so the
+// velocity sets compile in parallel).
+#include "lbm_batch.cuh"
+
+namespace lbm {
+LBM_BATCH_INSTANTIATE(q37, D2Q37)
+}  // namespace lbm

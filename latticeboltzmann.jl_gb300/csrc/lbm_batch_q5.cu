@@ -1,0 +1,7 @@
+// Batched step and reduction kernels for the D2Q5 velocity set (own translation unit, so the
+// velocity sets compile in parallel).
+#include "lbm_batch.cuh"
+
+namespace lbm {
+LBM_BATCH_INSTANTIATE(q5, D2Q5)
+}  // namespace lbm

@@ -1,0 +1,7 @@
+// Batched step and reduction kernels for the D2Q9 velocity set (own translation unit, so the
+// velocity sets compile in parallel).
+#include "lbm_batch.cuh"
+
+namespace lbm {
+LBM_BATCH_INSTANTIATE(q9, D2Q9)
+}  // namespace lbm

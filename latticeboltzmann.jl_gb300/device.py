@@ -227,7 +227,7 @@ class DeviceLattice:
 class DeviceBatch:
     """Several DeviceLattices advanced together: member k takes nsteps[k] steps, all issued as one
     CUDA graph with one kernel per global step over every member still running (lbm_batch_*).
-    Members must share storage and collision kind (SRT / TRT), use D2Q4..D2Q17 and no
+    Members must share storage (f64, df64dev or f32dev) and collision kind (SRT, TRT or MRT) and have no
     time-dependent force."""
 
     def __init__(self, lattices):
@@ -237,8 +237,8 @@ class DeviceBatch:
         h = C.c_void_p()
         st = L.lbm_batch_create(C.byref(h), arr, len(self.lattices))
         if st != N.LBM_OK:
-            raise N.LbmError(st, "lbm_batch_create: members must share storage and SRT/TRT collision, "
-                                 "use D2Q4..D2Q17 and no time-dependent force")
+            raise N.LbmError(st, "lbm_batch_create: members must share storage and collision kind (SRT, TRT, MRT), "
+                                 "use f64 / df64dev / f32dev and no time-dependent force")
         self.h = h
 
     def _check(self, st):

@@ -74,3 +74,32 @@ def test_small_tgv_convergence_study(lbm_gpu):
     assert res["max_rel_diff_batched_vs_sequential"] == 0.0
     for q, order in res["orders"].items():
         assert 1.5 < order < 3.0, (q, order)
+
+
+@pytest.mark.parametrize("storage", ["f64", "df64dev", "f32dev"])
+@pytest.mark.parametrize("coll", ["SRT", "TRT", "MRT"])
+def test_batch_every_velocity_set(lbm_gpu, storage, coll):
+    """One batch of all seven velocity sets (MRT included), uneven sizes and step counts, equal
+    bitwise to stepping each lattice alone."""
+    lbm = lbm_gpu
+    specs = [("D2Q4", 9, 7, 11), ("D2Q5", 12, 5, 3), ("D2Q9", 33, 20, 14), ("D2Q13", 17, 9, 0),
+             ("D2Q17", 20, 11, 6), ("D2Q21", 7, 13, 9), ("D2Q37", 25, 18, 5)]
+    models = {}
+    for mode in ("batch", "solo"):
+        ms = []
+        for k, (qn, nx, ny, n) in enumerate(specs):
+            q = lbm.Quadratures[qn]
+            f0 = wave_field(q, nx, ny, seed=300 + k, amp=0.01)
+            cm = {"SRT": lbm.SRT(0.75), "TRT": lbm.TRT.fields(0.75, 1.2), "MRT": lbm.MRT(q, 0.75)}[coll]
+            ms.append(lbm.LatticeBoltzmannModel.from_parts(q, f0, cm, storage=storage))
+        models[mode] = ms
+    steps = np.array([s[3] for s in specs], dtype=np.int64)
+    batch = lbm.DeviceBatch([m.lattice for m in models["batch"]])
+    batch.step(steps)
+    for m, n in zip(models["solo"], steps):
+        m.lattice.step(int(n), 0, 0.0)
+    for mb, ms, spec in zip(models["batch"], models["solo"], specs):
+        assert np.array_equal(mb.f_stream, ms.f_stream), spec
+    batch.close()
+    for m in models["batch"] + models["solo"]:
+        m.close()
