@@ -470,6 +470,16 @@ def main():
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6.8 TB/s",
                              "bytes_per_lu": bytes_lu, "kernel": "step_kernel<D2Q9,TRT,fused>"},
                 "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu}
+        fp64_inst = profiled_traffic().get("step_f64_fp64_thread_inst_per_lu")
+        if args.storage == "f64" and fp64_inst and clocks and clocks.get("sm_mhz"):
+            # the FP64 step's own roof: GB300 issues 2 FP64 thread instructions per SM per clock
+            peak = 152 * 2 * clocks["sm_mhz"] * 1e6 / 1e9
+            ach = fp64_inst * mlups * 1e6 / 1e9
+            line["compute_roofline"] = {"bound": "fp64 pipe", "achieved": ach, "peak": peak,
+                                        "unit": "G FP64 thread-instructions/s", "frac": ach / peak,
+                                        "instructions_per_lu": fp64_inst,
+                                        "peak_source": "152 SMs x 2 FP64 instructions per clock (rate measured with ncu) "
+                                                       "x median SM clock of the timed region"}
         line.update(extra)
         print(json.dumps(finite(line), allow_nan=False))
     if world > 1:
