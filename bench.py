@@ -256,6 +256,30 @@ def bench_trt_sweep(torch, lbm, every=40):
     return res
 
 
+def bench_all_sets(torch, lbm, n=2048, steps=40):
+    """Every velocity set, TRT, periodic n x n, zero-velocity start plus a constant force: the
+    fused step's MLUPS and fraction of the measured HBM bandwidth per storage (2 Q sizeof(T)
+    bytes per update)."""
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    out = {"workload": f"TRT periodic {n}x{n}, Fx = 1e-6, {steps} steps per storage and velocity set"}
+    for qn in ("D2Q4", "D2Q5", "D2Q9", "D2Q13", "D2Q17", "D2Q21", "D2Q37"):
+        q = lbm.Quadratures[qn]
+        row = {}
+        for storage, esize in (("f64", 8), ("df64dev", 8), ("f32dev", 4)):
+            lat = lbm.DeviceLattice(q, n, n, lbm.TRT.fields(0.8, 1.1), (), force=("constant", (1e-6, 0.0)),
+                                    storage=storage)
+            lat.initialize_fields()
+            m = type("M", (), {"lattice": lat})()
+            st = steps if storage != "f64" else max(4, steps // 4)
+            sec, _ = time_device(torch, m, st, 3, 0.0)
+            lat.close()
+            mlups = n * n * st / sec / 1e6
+            row[storage] = {"mlups": mlups, "hbm_frac": 2 * q.Q * esize * mlups * 1e6 / 1e9 / peak}
+        out[qn] = row
+    return out
+
+
 def bench_init(torch, lbm, n=2048):
     """Model construction with the Taylor-Green equilibrium + off-equilibrium initial condition:
     the state built on the device from the macroscopic planes, against the host build of all Q
@@ -450,7 +474,7 @@ def main():
     if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
         extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
                             "batched": bench_batched(torch, lbm), "trt_sweep": bench_trt_sweep(torch, lbm),
-                            "init": bench_init(torch, lbm),
+                            "init": bench_init(torch, lbm), "all_sets": bench_all_sets(torch, lbm),
                             "adjoint": bench_adjoint(torch, lbm)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
