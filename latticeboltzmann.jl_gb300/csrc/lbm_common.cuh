@@ -25,18 +25,29 @@ __device__ __forceinline__ void static_for(F&& f) {
   }
 }
 
+// Additions inside sums whose result feeds further arithmetic: plain for FP32 / FP64; for
+// float-float without the closing renormalisation (add_lazy, lbm_df64.cuh).
+template <class CT>
+__device__ __forceinline__ CT ladd(CT a, CT b) { return a + b; }
+template <class CT>
+__device__ __forceinline__ CT lsub(CT a, CT b) { return a - b; }
+#ifdef __CUDACC__
+__device__ __forceinline__ dd ladd(dd a, dd b) { return add_lazy(a, b); }
+__device__ __forceinline__ dd lsub(dd a, dd b) { return add_lazy(a, -b); }
+#endif
+
 // v (+)= C t for a compile-time integer C; the first term initialises v, since IEEE arithmetic
 // cannot fold a leading 0 + t away.  `set` is a constant at every point of an unrolled loop.
 template <int C, class CT>
 __device__ __forceinline__ void acc_add(CT& v, bool& set, CT t) {
   if constexpr (C == 1) {
-    v = set ? v + t : t;
+    v = set ? ladd(v, t) : t;
     set = true;
   } else if constexpr (C == -1) {
-    v = set ? v - t : -t;
+    v = set ? lsub(v, t) : -t;
     set = true;
   } else if constexpr (C != 0) {
-    v = set ? v + (CT)C * t : (CT)C * t;
+    v = set ? ladd(v, (CT)C * t) : (CT)C * t;
     set = true;
   }
 }

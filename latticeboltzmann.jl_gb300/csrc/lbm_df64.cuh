@@ -54,6 +54,15 @@ __device__ __forceinline__ dd operator+(dd a, dd b) {
   return fast_two_sum(s.hi, e);
 }
 
+// a + b without the closing renormalisation, for sums that feed further sums or products: the
+// leading parts are added exactly (two_sum) and every rounding error is kept in the trailing
+// part, so a chain of such additions is the cascaded summation of Ogita, Rump and Oishi
+// ("Accurate sum and dot product", 2005), renormalised by the first full addition after it.
+__device__ __forceinline__ dd add_lazy(dd a, dd b) {
+  const dd s = two_sum(a.hi, b.hi);
+  return dd(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
 __device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
 
 __device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }

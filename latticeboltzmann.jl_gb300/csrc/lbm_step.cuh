@@ -299,7 +299,7 @@ __device__ __forceinline__ void mrt_out_pair(const StepParams<CT>& p, const MrtC
     bool s1s = false;
     acc_add<L::cx(I)>(s1, s1s, c.B1p);
     acc_add<L::cy(I)>(s1, s1s, c.B2p);
-    wo = so ? wo + p.w1[I] * s1 : p.w1[I] * s1;
+    wo = so ? ladd(wo, p.w1[I] * s1) : p.w1[I] * s1;
   }
   out_i = we + wo;
   out_o = we - wo;
@@ -403,8 +403,8 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
     if constexpr (o == i) {
       acc_add<1>(drho, sr, v[i]);
     } else if constexpr (o > i) {
-      sp[i] = v[i] + v[o];
-      dp[i] = v[i] - v[o];
+      sp[i] = ladd(v[i], v[o]);
+      dp[i] = lsub(v[i], v[o]);
       acc_add<1>(drho, sr, sp[i]);
     }
   });
@@ -463,8 +463,8 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
       acc_add<L::cy(i)>(X, xs, jy);
       [[maybe_unused]] const CT X2 = X * X;
       CT Se = b0[k];
-      if constexpr (L::EQ >= 4) Se = Se + X2 * (b2[k] + X2 * b4[k]);
-      else if constexpr (L::EQ >= 2) Se = Se + X2 * b2[k];
+      if constexpr (L::EQ >= 4) Se = ladd(Se, X2 * ladd(b2[k], X2 * b4[k]));
+      else if constexpr (L::EQ >= 2) Se = ladd(Se, X2 * b2[k]);
       CT Ya;
       if constexpr (F32) {
         CT A = p.w1[i] * X;
@@ -472,10 +472,10 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
         Ya = p.pa_a * dp[i] + p.pom_a * A;
       } else {
         CT t = p.pw1a[i];
-        if constexpr (L::EQ >= 3) t += a3[k] * (csq * X2 - cs3J2);
-        Ya = p.pa_a * dp[i] + t * X;
+        if constexpr (L::EQ >= 3) t = ladd(t, a3[k] * lsub(csq * X2, cs3J2));
+        Ya = ladd(p.pa_a * dp[i], t * X);
       }
-      const CT Ys = p.pa_s * sp[i] + Se;
+      const CT Ys = ladd(p.pa_s * sp[i], Se);
       v[i] = Ys + Ya;
       v[o] = Ys - Ya;
     }
