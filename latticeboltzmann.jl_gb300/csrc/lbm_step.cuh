@@ -215,17 +215,15 @@ __device__ __forceinline__ void mrt_accumulate_pair(CT* M, bool* set, CT s, CT d
 template <class L, bool DEV, class CT>
 __device__ __forceinline__ void mrt_coeffs(const StepParams<CT>& p, const CT* M, CT sFx, CT sFy, bool has_force,
                                            MrtCoeffs<CT>& c) {
-  const CT rho = DEV ? (CT)1 + M[0] : M[0];
+  const CT rho = DEV ? ladd((CT)1, M[0]) : M[0];
   const CT inv_rho = (CT)1 / rho;
   CT ux = M[1] * inv_rho, uy = M[2] * inv_rho;
   if (has_force) {
-    ux += sFx;
-    uy += sFy;
+    ux = ladd(ux, sFx);
+    uy = ladd(uy, sFy);
   }
   const CT cs = p.cs, ics = (CT)1 / cs;  // ics = c_s^2
-  CT* B = c.B;
-#pragma unroll
-  for (int k = 0; k < 15; ++k) B[k] = 0;
+  CT* B = c.B;  // every coefficient is assigned before it is updated (no 0 + x)
   B[0] = M[0];  // ρ, or ρ - 1 in deviation form
   B[1] = cs * rho * ux;
   B[2] = cs * rho * uy;
@@ -233,49 +231,50 @@ __device__ __forceinline__ void mrt_coeffs(const StepParams<CT>& p, const CT* M,
   c.B2p = rho * uy;
   if constexpr (L::HN >= 2) {
     const CT a = p.mrt_a[1], b = p.mrt_b[1];
-    const CT Axx = a * (M[3] - ics * M[0]) + b * (rho * ux * ux);
-    const CT Axy = a * M[4] + b * (rho * ux * uy);
-    const CT Ayy = a * (M[5] - ics * M[0]) + b * (rho * uy * uy);
+    const CT Axx = ladd(a * lsub(M[3], ics * M[0]), b * (rho * ux * ux));
+    const CT Axy = ladd(a * M[4], b * (rho * ux * uy));
+    const CT Ayy = ladd(a * lsub(M[5], ics * M[0]), b * (rho * uy * uy));
     const CT c2 = cs * cs * (CT)0.5;
-    B[3] += c2 * Axx;
-    B[4] += c2 * (CT)2 * Axy;
-    B[5] += c2 * Ayy;
-    B[0] -= c2 * ics * (Axx + Ayy);
+    B[3] = c2 * Axx;
+    B[4] = c2 * (CT)2 * Axy;
+    B[5] = c2 * Ayy;
+    B[0] = lsub(B[0], c2 * ics * ladd(Axx, Ayy));
   }
   if constexpr (L::HN >= 3) {
     const CT a = p.mrt_a[2], b = p.mrt_b[2];
-    const CT Axxx = a * (M[6] - (CT)3 * ics * M[1]) + b * (rho * ux * ux * ux);
-    const CT Axxy = a * (M[7] - ics * M[2]) + b * (rho * ux * ux * uy);
-    const CT Axyy = a * (M[8] - ics * M[1]) + b * (rho * ux * uy * uy);
-    const CT Ayyy = a * (M[9] - (CT)3 * ics * M[2]) + b * (rho * uy * uy * uy);
+    const CT Axxx = ladd(a * lsub(M[6], (CT)3 * ics * M[1]), b * (rho * ux * ux * ux));
+    const CT Axxy = ladd(a * lsub(M[7], ics * M[2]), b * (rho * ux * ux * uy));
+    const CT Axyy = ladd(a * lsub(M[8], ics * M[1]), b * (rho * ux * uy * uy));
+    const CT Ayyy = ladd(a * lsub(M[9], (CT)3 * ics * M[2]), b * (rho * uy * uy * uy));
     const CT c3 = cs * cs * cs * (CT)(1.0 / 6.0);
-    B[6] += c3 * Axxx;
-    B[7] += c3 * (CT)3 * Axxy;
-    B[8] += c3 * (CT)3 * Axyy;
-    B[9] += c3 * Ayyy;
-    B[1] -= c3 * (CT)3 * ics * (Axxx + Axyy);
-    B[2] -= c3 * (CT)3 * ics * (Axxy + Ayyy);
-    c.B1p -= c3 * (CT)3 * ics * ics * (Axxx + Axyy);
-    c.B2p -= c3 * (CT)3 * ics * ics * (Axxy + Ayyy);
+    B[6] = c3 * Axxx;
+    B[7] = c3 * (CT)3 * Axxy;
+    B[8] = c3 * (CT)3 * Axyy;
+    B[9] = c3 * Ayyy;
+    const CT sx = ladd(Axxx, Axyy), sy = ladd(Axxy, Ayyy);
+    B[1] = lsub(B[1], c3 * (CT)3 * ics * sx);
+    B[2] = lsub(B[2], c3 * (CT)3 * ics * sy);
+    c.B1p = lsub(c.B1p, c3 * (CT)3 * ics * ics * sx);
+    c.B2p = lsub(c.B2p, c3 * (CT)3 * ics * ics * sy);
   }
   if constexpr (L::HN >= 4) {
     const CT a = p.mrt_a[3], b = p.mrt_b[3];
     const CT ics2 = ics * ics;
-    const CT Axxxx = a * (M[10] - (CT)6 * ics * M[3] + (CT)3 * ics2 * M[0]) + b * (rho * ux * ux * ux * ux);
-    const CT Axxxy = a * (M[11] - (CT)3 * ics * M[4]) + b * (rho * ux * ux * ux * uy);
-    const CT Axxyy = a * (M[12] - ics * (M[3] + M[5]) + ics2 * M[0]) + b * (rho * ux * ux * uy * uy);
-    const CT Axyyy = a * (M[13] - (CT)3 * ics * M[4]) + b * (rho * ux * uy * uy * uy);
-    const CT Ayyyy = a * (M[14] - (CT)6 * ics * M[5] + (CT)3 * ics2 * M[0]) + b * (rho * uy * uy * uy * uy);
+    const CT Axxxx = ladd(a * ladd(lsub(M[10], (CT)6 * ics * M[3]), (CT)3 * ics2 * M[0]), b * (rho * ux * ux * ux * ux));
+    const CT Axxxy = ladd(a * lsub(M[11], (CT)3 * ics * M[4]), b * (rho * ux * ux * ux * uy));
+    const CT Axxyy = ladd(a * ladd(lsub(M[12], ics * ladd(M[3], M[5])), ics2 * M[0]), b * (rho * ux * ux * uy * uy));
+    const CT Axyyy = ladd(a * lsub(M[13], (CT)3 * ics * M[4]), b * (rho * ux * uy * uy * uy));
+    const CT Ayyyy = ladd(a * ladd(lsub(M[14], (CT)6 * ics * M[5]), (CT)3 * ics2 * M[0]), b * (rho * uy * uy * uy * uy));
     const CT c4 = cs * cs * cs * cs * (CT)(1.0 / 24.0);
-    B[10] += c4 * Axxxx;
-    B[11] += c4 * (CT)4 * Axxxy;
-    B[12] += c4 * (CT)6 * Axxyy;
-    B[13] += c4 * (CT)4 * Axyyy;
-    B[14] += c4 * Ayyyy;
-    B[3] -= c4 * ics * (CT)6 * (Axxxx + Axxyy);
-    B[4] -= c4 * ics * (CT)12 * (Axxxy + Axyyy);
-    B[5] -= c4 * ics * (CT)6 * (Axxyy + Ayyyy);
-    B[0] += c4 * ics2 * ((CT)3 * Axxxx + (CT)6 * Axxyy + (CT)3 * Ayyyy);
+    B[10] = c4 * Axxxx;
+    B[11] = c4 * (CT)4 * Axxxy;
+    B[12] = c4 * (CT)6 * Axxyy;
+    B[13] = c4 * (CT)4 * Axyyy;
+    B[14] = c4 * Ayyyy;
+    B[3] = lsub(B[3], c4 * ics * (CT)6 * ladd(Axxxx, Axxyy));
+    B[4] = lsub(B[4], c4 * ics * (CT)12 * ladd(Axxxy, Axyyy));
+    B[5] = lsub(B[5], c4 * ics * (CT)6 * ladd(Axxyy, Ayyyy));
+    B[0] = ladd(B[0], c4 * ics2 * ladd(ladd((CT)3 * Axxxx, (CT)6 * Axxyy), (CT)3 * Ayyyy));
   }
 }
 
@@ -417,17 +416,17 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
   });
   // FP64 storage holds f, so `drho` is ρ itself and w·drho below is w ρ; deviation storage
   // holds g = f - w, so it is ρ - 1 and w·drho is the deviation w (ρ - 1) of the rest state
-  const CT rho = DEV ? (CT)1 + drho : drho;
+  const CT rho = DEV ? ladd((CT)1, drho) : drho;
   const CT inv = pair_recip(rho);
   if (has_force) {  // j' = ρ (u + τ F)
-    jx += rho * sFx;
-    jy += rho * sFy;
+    jx = ladd(jx, rho * sFx);
+    jy = ladd(jy, rho * sFy);
   }
   // node-wide, weight-free factors of b0, b2, b4 and a3
   CT D0 = drho, D2 = 0, D4 = 0, J2 = 0, c3 = 0, cs3J2 = 0, csq = 0;
   if constexpr (L::EQ >= 2) {
-    J2 = jx * jx + jy * jy;
-    D0 = drho - (p.hcs * J2) * inv;
+    J2 = ladd(jx * jx, jy * jy);
+    D0 = lsub(drho, (p.hcs * J2) * inv);
     D2 = p.hcs2 * inv;
   }
   if constexpr (L::EQ >= 3) {
@@ -437,8 +436,8 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
   }
   if constexpr (L::EQ >= 4) {
     const CT c4 = (CT)(1.0 / 24.0) * (inv * inv) * inv;  // 1 / (24 ρ³)
-    D0 += ((CT)3 * csq) * (J2 * J2) * c4;
-    D2 -= ((CT)6 * (csq * p.cs)) * J2 * c4;
+    D0 = ladd(D0, ((CT)3 * csq) * (J2 * J2) * c4);
+    D2 = lsub(D2, ((CT)6 * (csq * p.cs)) * J2 * c4);
     D4 = (csq * csq) * c4;
   }
   CT b0[16], b2[16], b4[16], a3[16];

