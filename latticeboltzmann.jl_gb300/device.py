@@ -27,7 +27,7 @@ class DeviceLattice:
 
     force: None | ("constant", (Fx, Fy)) | ("field", array (2, NY, NX)) |
            ("shear", [c0..c5], x_coords, y_coords)
-    storage: "f64" | "f32dev" | "f16dev"
+    storage: "f64" | "df64dev" (float-float deviation) | "f32dev" | "f16dev"
     nonlinear: the (Q, NY, NX) term of the iterative-initialisation collision model
     """
 
