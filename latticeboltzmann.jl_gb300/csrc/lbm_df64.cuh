@@ -89,6 +89,8 @@ __device__ __forceinline__ dd recip(dd b) {
 
 __device__ __forceinline__ dd operator/(dd a, dd b) { return a * recip(b); }
 
+__device__ __forceinline__ bool operator!=(dd a, dd b) { return a.hi != b.hi || a.lo != b.lo; }
+
 __device__ __forceinline__ dd& operator+=(dd& a, dd b) { return a = a + b; }
 __device__ __forceinline__ dd& operator-=(dd& a, dd b) { return a = a - b; }
 __device__ __forceinline__ dd& operator*=(dd& a, dd b) { return a = a * b; }

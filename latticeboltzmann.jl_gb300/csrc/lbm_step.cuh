@@ -359,11 +359,26 @@ __device__ __forceinline__ void mrt_collide(const StepParams<CT>& p, CT* v, CT s
 // Newton-Raphson step r (2 - ρ r), relative error ~1e-14, well below what the terms it scales
 // (u² ~ 1e-4 of f) need; FP32: the hardware reciprocal; float-float: recip() of lbm_df64.cuh.
 __device__ __forceinline__ double pair_recip(double r) {
-  const double r0 = (double)__frcp_rn((float)r);
-  return fma(r0, fma(-r, r0, 1.0), r0);
+  // the float approximation is formed from the bits of r (no FP64-pipe conversions): exponent
+  // rebiased, significand truncated to 23 bits; densities lie well inside float's exponent range,
+  // anything else (≤ 0, tiny, huge, NaN) takes the full division
+  const long long b = __double_as_longlong(r);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (b > 0 && e > 1023 - 120 && e < 1023 + 120) {
+    const float rf = __int_as_float(((e - 1023 + 127) << 23) | (int)((b >> 29) & 0x7FFFFF));
+    const int rb = __float_as_int(__frcp_rn(rf));
+    const double r0 =
+        __longlong_as_double(((long long)(((rb >> 23) & 0xFF) - 127 + 1023) << 52) | ((long long)(rb & 0x7FFFFF) << 29));
+    return fma(r0, fma(-r, r0, 1.0), r0);
+  }
+  return 1.0 / r;
 }
 __device__ __forceinline__ float pair_recip(float r) { return __frcp_rn(r); }
 __device__ __forceinline__ dd pair_recip(dd r) { return recip(r); }
+
+__device__ __forceinline__ bool nonzero_bits(double v) { return __double_as_longlong(v) != 0; }
+__device__ __forceinline__ bool nonzero_bits(float v) { return __float_as_int(v) != 0; }
+__device__ __forceinline__ bool nonzero_bits(dd v) { return __float_as_int(v.hi) != 0 || __float_as_int(v.lo) != 0; }
 
 // Velocity class of population i: the set {(±a, ±b), (±b, ±a)}, which shares one weight.
 template <class L>
@@ -418,9 +433,9 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
   // holds g = f - w, so it is ρ - 1 and w·drho is the deviation w (ρ - 1) of the rest state
   const CT rho = DEV ? ladd((CT)1, drho) : drho;
   const CT inv = pair_recip(rho);
-  if (has_force) {  // j' = ρ (u + τ F)
-    jx = ladd(jx, rho * sFx);
-    jy = ladd(jy, rho * sFy);
+  if (has_force) {  // j' = ρ (u + τ F); a zero component adds nothing (tested on its bits, not on the FP64 pipe)
+    if (nonzero_bits(sFx)) jx = ladd(jx, rho * sFx);
+    if (nonzero_bits(sFy)) jy = ladd(jy, rho * sFy);
   }
   // node-wide, weight-free factors of b0, b2, b4 and a3
   CT D0 = drho, D2 = 0, D4 = 0, J2 = 0, c3 = 0, cs3J2 = 0, csq = 0;
