@@ -1,0 +1,73 @@
+"""Error behaviour of the C ABI on a live context: every misuse returns its documented status,
+records a message, and leaves the context usable."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gpu_cases import wave_field
+
+pytestmark = pytest.mark.gpu
+
+
+def _lattice(lbm, qname="D2Q9", storage="f64", cm=None, nx=12, ny=10):
+    q = lbm.Quadratures[qname]
+    return lbm.DeviceLattice(q, nx, ny, cm or lbm.TRT.fields(0.8, 1.1), (), storage=storage)
+
+
+def test_state_and_argument_errors(lbm_gpu):
+    lbm = lbm_gpu
+    N = lbm._native
+    L = N.lib()
+    lat = _lattice(lbm)
+    assert L.lbm_step(lat.h, 3, 0, 0.0) == N.LBM_ERR_STATE            # nothing uploaded yet
+    assert b"no state" in L.lbm_last_error(lat.h)
+    out = np.zeros(16)
+    assert L.lbm_reduce(lat.h, N.REDUCE_CONSERVED, None, out.ctypes.data_as(N._DP)) == N.LBM_ERR_STATE
+    lat.initialize_fields()
+    assert L.lbm_step(lat.h, -1, 0, 0.0) == N.LBM_ERR_INVALID
+    assert L.lbm_reduce(lat.h, 99, None, out.ctypes.data_as(N._DP)) == N.LBM_ERR_INVALID
+    assert L.lbm_reduce(lat.h, N.REDUCE_TRACK_ERRORS, None, out.ctypes.data_as(N._DP)) == N.LBM_ERR_INVALID
+    out[0], out[1] = 12, 0  # node x out of range
+    assert L.lbm_reduce(lat.h, N.REDUCE_DENSITY_AT, None, out.ctypes.data_as(N._DP)) == N.LBM_ERR_INVALID
+    sxx = np.zeros((10, 12))
+    assert L.lbm_initialize_fields(lat.h, None, None, None, None, sxx.ctypes.data_as(N._DP), None, None, 1.0,
+                                   0) == N.LBM_ERR_INVALID
+    # the context is still usable
+    lat.step(5)
+    assert abs(lat.conserved()[0] - 12 * 10) < 1e-12
+    lat.close()
+
+
+def test_non_finite_populations_are_reported(lbm_gpu):
+    lbm = lbm_gpu
+    N = lbm._native
+    lat = _lattice(lbm)
+    f = np.ascontiguousarray(wave_field(lbm.D2Q9(), 12, 10, seed=3))
+    f[4, 3, 5] = np.nan
+    lat.upload(f)
+    with pytest.raises(N.LbmError) as e:
+        lat.conserved()
+    assert e.value.status == N.LBM_ERR_NONFINITE
+    lat.close()
+
+
+def test_unsupported_combinations(lbm_gpu):
+    lbm = lbm_gpu
+    N = lbm._native
+    L = N.lib()
+    a = _lattice(lbm, storage="f64")
+    b = _lattice(lbm, storage="f32dev")
+    with pytest.raises(N.LbmError):            # members must share the storage
+        lbm.DeviceBatch([a, b])
+    c = _lattice(lbm, cm=lbm.SRT(0.8))
+    with pytest.raises(N.LbmError):            # ... and the collision kind
+        lbm.DeviceBatch([a, c])
+    h = C.c_void_p()
+    d17 = _lattice(lbm, "D2Q17")
+    assert L.lbm_adjoint_create(C.byref(h), d17.h, 10, 0) == N.LBM_ERR_UNSUPPORTED
+    assert b"adjoint" in L.lbm_last_error(d17.h)
+    f16 = _lattice(lbm, storage="f16dev")
+    assert L.lbm_collide_device(f16.h, None, None, 0.0) in (N.LBM_ERR_INVALID, N.LBM_ERR_UNSUPPORTED)
+    for lat in (a, b, c, d17, f16):
+        lat.close()
