@@ -781,11 +781,17 @@ int32_t lbm_reduce(lbm_ctx* c, int32_t kind, const lbm_analytic* an, double* out
     } else {
       int rc = ensure(c, &c->d_analytic, (size_t)c->n * 8 * sizeof(double));
       if (rc) return rc;
-      for (int k = 0; k < 8; ++k) {
-        dptr[k] = c->d_analytic + (size_t)k * c->n;
-        if (src[k])
-          LBM_CUDA(c, cudaMemcpyAsync((void*)dptr[k], src[k], (size_t)c->n * sizeof(double), cudaMemcpyHostToDevice,
-                                      c->stream));
+      bool one_block = true;  // the eight planes consecutive in one host array: one copy
+      for (int k = 0; k < 8; ++k) one_block = one_block && src[k] == src[0] + (size_t)k * c->n;
+      for (int k = 0; k < 8; ++k) dptr[k] = c->d_analytic + (size_t)k * c->n;
+      if (one_block) {
+        LBM_CUDA(c, cudaMemcpyAsync(c->d_analytic, src[0], (size_t)c->n * 8 * sizeof(double), cudaMemcpyHostToDevice,
+                                    c->stream));
+      } else {
+        for (int k = 0; k < 8; ++k)
+          if (src[k])
+            LBM_CUDA(c, cudaMemcpyAsync((void*)dptr[k], src[k], (size_t)c->n * sizeof(double), cudaMemcpyHostToDevice,
+                                        c->stream));
       }
     }
     r.rho_a = dptr[0];

@@ -19,6 +19,7 @@ reference's tests do (test/initial_conditions.jl:12-87).
 """
 from __future__ import annotations
 
+import functools
 import math
 
 import numpy as np
@@ -104,14 +105,35 @@ def _linspace(a: float, b: float, n: int):
     return vals, float(st)
 
 
+def _ranges(NX, NY, d0, d1):
+    """Node coordinates of a lattice; small lattices (the points of a sweep share them) are cached."""
+    if NX * NY <= 1 << 16:
+        return _ranges_cached(NX, NY, d0, d1)
+    return _ranges_build(NX, NY, d0, d1)
+
+
+@functools.lru_cache(maxsize=512)
+def _ranges_cached(NX, NY, d0, d1):
+    return _ranges_build(NX, NY, d0, d1)
+
+
+def _ranges_build(NX, NY, d0, d1):
+    dx = d0 / NX
+    dy = d1 / NY
+    xr, xs = _linspace(dx / 2, d0 - dx / 2, NX)
+    yr, ys = _linspace(dy / 2, d0 - dy / 2, NY)
+    X, Y = np.meshgrid(xr, yr)
+    for a in (xr, yr, X, Y):
+        a.setflags(write=False)  # shared between problems of one shape
+    return xr, yr, xs, ys, X, Y
+
+
 def problem_range(problem):
     """The reference's range(problem) (problems.jl:18-26): cell-centred node coordinates.
     Like the reference, the y range ends at domain_size[1] - Δy/2 using the FIRST domain
     extent.  Returns (x_range, y_range, x_step, y_step)."""
-    dx = problem.domain_size[0] / problem.NX
-    dy = problem.domain_size[1] / problem.NY
-    xr, xs = _linspace(dx / 2, problem.domain_size[0] - dx / 2, problem.NX)
-    yr, ys = _linspace(dy / 2, problem.domain_size[0] - dy / 2, problem.NY)
+    xr, yr, xs, ys, _, _ = _ranges(int(problem.NX), int(problem.NY), float(problem.domain_size[0]),
+                                   float(problem.domain_size[1]))
     return xr, yr, xs, ys
 
 
@@ -159,9 +181,8 @@ def lattice_temperature(q, problem, x, y, t=0.0):
 
 def node_grid(problem):
     """Coordinate arrays X, Y of shape (NY, NX) (row y, column x)."""
-    xr, yr, _, _ = problem_range(problem)
-    X, Y = np.meshgrid(xr, yr)
-    return X, Y
+    return _ranges(int(problem.NX), int(problem.NY), float(problem.domain_size[0]),
+                   float(problem.domain_size[1]))[4:]
 
 
 def lattice_force_field(problem, t=0.0):
@@ -184,9 +205,10 @@ def analytic_fields(q, problem, t):
     ux, uy = problem.velocity(X, Y, t)
     p = np.broadcast_to(problem.pressure(q, X, Y, t), X.shape).astype(np.float64)
     s = problem.deviatoric_tensor(q, X, Y, t)
-    b = lambda a: np.ascontiguousarray(np.broadcast_to(a, X.shape), dtype=np.float64)
-    return {"rho": b(rho), "ux": b(ux), "uy": b(uy), "p": b(p), "sxx": b(s[0, 0]), "syx": b(s[1, 0]),
-            "sxy": b(s[0, 1]), "syy": b(s[1, 1])}
+    out = np.empty((8,) + X.shape)  # one block, so the eight planes travel in one copy
+    for k, a in enumerate((rho, ux, uy, p, s[0, 0], s[1, 0], s[0, 1], s[1, 1])):
+        out[k] = a
+    return dict(zip(("rho", "ux", "uy", "p", "sxx", "syx", "sxy", "syy"), out))
 
 
 # ---------------------------------------------------------------------------------------
