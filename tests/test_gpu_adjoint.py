@@ -117,3 +117,32 @@ def test_fp32_adjoint_close_to_fp64(lbm_gpu):
     assert r["f32dev"]["loss"] == pytest.approx(r["f64"]["loss"], rel=1e-4)
     g64, g32 = r["f64"]["grad_u0"], r["f32dev"]["grad_u0"]
     assert np.max(np.abs(g32 - g64)) <= 1e-3 * np.max(np.abs(g64))
+
+
+def test_autograd_function_returns_the_adjoint_gradients(lbm_gpu):
+    """LBMLoss (the torch.autograd counterpart of a ChainRulesCore.rrule for this loss): its
+    backward gives the adjoint's ∂L/∂u0, the total ∂L/∂τ_s along the magic relation and ∂L/∂F,
+    and a gradient step on u0 lowers the loss."""
+    torch = pytest.importorskip("torch")
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    q = lbm.D2Q9()
+
+    def factory(tau, F):
+        return lbm.AdjointProblem(q, NX, NY, lbm.TRT.fields(tau, lbm.trt_magic(tau)), force=F, nsteps=STEPS)
+
+    u = torch.tensor(u0, dtype=torch.float64, requires_grad=True)
+    tau = torch.tensor(0.8, dtype=torch.float64, requires_grad=True)
+    F = torch.tensor([2e-6, -1e-6], dtype=torch.float64, requires_grad=True)
+    loss = lbm.LBMLoss.apply(u, tau, F, factory, ut)
+    loss.backward()
+    prob = factory(0.8, (2e-6, -1e-6))
+    ref = prob.run(u0, ut)
+    prob.close()
+    assert float(loss.detach()) == ref["loss"]
+    np.testing.assert_array_equal(u.grad.numpy(), ref["grad_u0"])
+    assert float(tau.grad) == pytest.approx(lbm.magic_total_derivative(ref, 0.8), rel=1e-12)
+    np.testing.assert_allclose(F.grad.numpy(), np.asarray(ref["dF"]), rtol=1e-12)
+    with torch.no_grad():
+        u_step = u - 1e-3 * u.grad / u.grad.abs().max()
+    assert float(lbm.LBMLoss.apply(u_step, tau, F, factory, ut).detach()) < float(loss.detach())
