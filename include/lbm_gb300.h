@@ -240,6 +240,12 @@ const char* lbm_batch_last_error(const lbm_batch* batch);
  * doubles, row k being what lbm_reduce(member k, kind) returns (zeros for members not selected;
  * CONSERVED: row k[3] counts non-finite populations instead of failing).  Synchronous. */
 int32_t lbm_batch_reduce(lbm_batch* batch, int32_t kind, const uint8_t* select, double* out);
+/* The error norms with analytic fields (LBM_REDUCE_TRACK_ERRORS, _COMPARE) of the selected members
+ * at once, e.g. the final TrackHydrodynamicErrors rows of a sweep (track_hydrodynamic_errors.jl:52-242):
+ * analytic[k] is member k's lbm_analytic with host planes, as lbm_reduce takes it (entries of
+ * members not selected are not read); out as for lbm_batch_reduce.  Synchronous. */
+int32_t lbm_batch_reduce_fields(lbm_batch* batch, int32_t kind, const uint8_t* select, const lbm_analytic* analytic,
+                                double* out);
 /* Members issue their own calls on the batch's stream until the batch is destroyed (no ordering
  * between streams per batch call; members must outlive the batch). */
 int32_t lbm_batch_share_stream(lbm_batch* batch);

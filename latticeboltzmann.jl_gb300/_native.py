@@ -125,6 +125,8 @@ def lib():
         L.lbm_initialize_fields.restype = C.c_int32
         L.lbm_batch_reduce.argtypes = [vp, C.c_int32, C.POINTER(C.c_uint8), _DP]
         L.lbm_batch_reduce.restype = C.c_int32
+        L.lbm_batch_reduce_fields.argtypes = [vp, C.c_int32, C.POINTER(C.c_uint8), C.POINTER(LbmAnalytic), _DP]
+        L.lbm_batch_reduce_fields.restype = C.c_int32
         L.lbm_batch_share_stream.argtypes = [vp]
         L.lbm_batch_share_stream.restype = C.c_int32
         L.lbm_adjoint_create.argtypes = [C.POINTER(vp), vp, C.c_int64, C.c_int64]
@@ -145,7 +147,7 @@ EXPORTED_SYMBOLS = [
     "lbm_download_device", "lbm_step", "lbm_last_launch_count", "lbm_reduce", "lbm_macroscopic",
     "lbm_collide_device", "lbm_stream_device", "lbm_apply_bcs_device", "lbm_batch_create", "lbm_batch_destroy",
     "lbm_batch_step", "lbm_batch_set_stream", "lbm_batch_synchronize", "lbm_batch_last_launch_count",
-    "lbm_batch_last_error", "lbm_batch_reduce", "lbm_batch_share_stream", "lbm_initialize_fields", "lbm_adjoint_create", "lbm_adjoint_destroy", "lbm_adjoint_run",
+    "lbm_batch_last_error", "lbm_batch_reduce", "lbm_batch_reduce_fields", "lbm_batch_share_stream", "lbm_initialize_fields", "lbm_adjoint_create", "lbm_adjoint_destroy", "lbm_adjoint_run",
     "lbm_adjoint_last_error",
 ]
 

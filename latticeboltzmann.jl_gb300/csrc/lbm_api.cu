@@ -898,6 +898,11 @@ struct lbm_batch {
   BatchDyn* h_dyn = nullptr;      // pinned staging copy
   cudaEvent_t staged = nullptr;   // the last upload from h_dyn has completed
   ReduceArgs* d_rargs = nullptr;  // per member, set up by the first reduction
+  std::vector<ReduceArgs> h_rargs; // host copy of the same
+  ReduceArgs* d_rargs_call = nullptr;  // per member, with this call's analytic fields
+  double* h_ranal = nullptr;       // pinned staging of the analytic planes
+  double* d_ranal = nullptr;
+  size_t ranal_cap = 0;            // doubles
   double* d_rpartial = nullptr;
   long long rpartial_blocks = 0;
   double* d_rout = nullptr;       // count x kRedMaxK
@@ -1022,6 +1027,9 @@ void lbm_batch_destroy(lbm_batch* b) {
   cudaFree(b->d_static);
   cudaFree(b->d_dyn);
   cudaFree(b->d_rargs);
+  cudaFree(b->d_rargs_call);
+  cudaFree(b->d_ranal);
+  if (b->h_ranal) cudaFreeHost(b->h_ranal);
   cudaFree(b->d_rpartial);
   cudaFree(b->d_rout);
   if (b->h_dyn) cudaFreeHost(b->h_dyn);
@@ -1169,42 +1177,36 @@ int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
   return batch_release_members(b);
 }
 
-// The reductions lbm_reduce computes without analytic fields (MEAN_VELOCITY,
-// VELOCITY_CONVERGENCE, CONSERVED) for every member at once: out[k * 16 + j] is what
-// lbm_reduce(member k, kind) would return in out[j].  One launch per velocity set plus one
-// fixed-order finish; VELOCITY_CONVERGENCE updates each member's previous-velocity planes as
-// lbm_reduce does.  CONSERVED reports the non-finite population count in out[k * 16 + 3].
-int32_t lbm_batch_reduce(lbm_batch* b, int32_t kind, const uint8_t* select, double* out) {
-  if (!b || !out) return LBM_ERR_INVALID;
-  if (kind != LBM_REDUCE_MEAN_VELOCITY && kind != LBM_REDUCE_VELOCITY_CONVERGENCE && kind != LBM_REDUCE_CONSERVED)
-    return bfail(b, LBM_ERR_UNSUPPORTED, "batched reductions: MEAN_VELOCITY, VELOCITY_CONVERGENCE, CONSERVED");
-  cudaSetDevice(b->device);
+}  // extern "C"
+
+namespace {
+
+// Per-member reduction arguments (weights, 1/c_s², previous-velocity planes), built once.
+int batch_ensure_rargs(lbm_batch* b) {
+  if (b->d_rargs) return LBM_OK;
   const int count = (int)b->members.size();
-  for (lbm_ctx* c : b->members)
-    if (!c->have_state) return bfail(b, LBM_ERR_STATE, "member without uploaded state");
-  int rc = batch_wait_members(b);
-  if (rc) return rc;
-  if (!b->d_rargs) {  // per-member reduction arguments (weights, 1/c_s², previous-velocity planes)
-    std::vector<ReduceArgs> ra(count);
-    for (int k = 0; k < count; ++k) {
-      lbm_ctx* c = b->members[k];
-      if (!c->d_uold) {
-        if (ensure(c, &c->d_uold, (size_t)c->n * 2 * sizeof(double))) return bfail(b, LBM_ERR_NOMEM, c->err);
-        if (cudaMemsetAsync(c->d_uold, 0, (size_t)c->n * 2 * sizeof(double), b->stream) != cudaSuccess)
-          return bfail(b, LBM_ERR_CUDA, "previous-velocity planes");
-      }
-      ra[k] = c->red;
-      ra[k].u_old = c->d_uold;
+  b->h_rargs.resize(count);
+  for (int k = 0; k < count; ++k) {
+    lbm_ctx* c = b->members[k];
+    if (!c->d_uold) {
+      if (ensure(c, &c->d_uold, (size_t)c->n * 2 * sizeof(double))) return bfail(b, LBM_ERR_NOMEM, c->err);
+      if (cudaMemsetAsync(c->d_uold, 0, (size_t)c->n * 2 * sizeof(double), b->stream) != cudaSuccess)
+        return bfail(b, LBM_ERR_CUDA, "previous-velocity planes");
     }
-    if (cudaMalloc((void**)&b->d_rargs, sizeof(ReduceArgs) * count) != cudaSuccess)
-      return bfail(b, LBM_ERR_NOMEM, "reduction arguments");
-    if (cudaMemcpy(b->d_rargs, ra.data(), sizeof(ReduceArgs) * count, cudaMemcpyHostToDevice) != cudaSuccess)
-      return bfail(b, LBM_ERR_CUDA, "reduction arguments");
+    b->h_rargs[k] = c->red;
+    b->h_rargs[k].u_old = c->d_uold;
   }
-  const int K = red_kind_k(kind);
-  std::vector<int> order;
-  for (int k = 0; k < count; ++k)
-    if (!select || select[k]) order.push_back(k);
+  if (cudaMalloc((void**)&b->d_rargs, sizeof(ReduceArgs) * count) != cudaSuccess)
+    return bfail(b, LBM_ERR_NOMEM, "reduction arguments");
+  if (cudaMemcpy(b->d_rargs, b->h_rargs.data(), sizeof(ReduceArgs) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bfail(b, LBM_ERR_CUDA, "reduction arguments");
+  return LBM_OK;
+}
+
+// The selected members' K sums of one reduction kind, with the arguments array `args`.
+int batch_reduce_run(lbm_batch* b, int K, const std::vector<int>& selected, const ReduceArgs* args, double* out) {
+  const int count = (int)b->members.size();
+  std::vector<int> order = selected;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int c) { return b->members[a]->qid < b->members[c]->qid; });
   const int nsel = (int)order.size();
@@ -1243,13 +1245,13 @@ int32_t lbm_batch_reduce(lbm_batch* b, int32_t kind, const uint8_t* select, doub
     }
     b->rpartial_blocks = total;
   }
-  rc = batch_upload_dyn(b, dyn);
+  int rc = batch_upload_dyn(b, dyn);
   if (rc) return rc;
   for (size_t gi = 0; gi + 1 < group_begin.size(); ++gi) {
     const int g0 = group_begin[gi], n = group_begin[gi + 1] - g0;
     const long long blocks = dyn[group_begin[gi + 1] - 1].block_start + dyn[group_begin[gi + 1] - 1].steps;
-    cudaError_t e = batch_reduce_launch(b->storage, b->members[order[g0]]->qid, K, b->d_static, b->d_rargs,
-                                        b->d_dyn + g0, n, blocks, b->d_rpartial, group_base[gi], b->d_rout, b->stream);
+    cudaError_t e = batch_reduce_launch(b->storage, b->members[order[g0]]->qid, K, b->d_static, args, b->d_dyn + g0, n,
+                                        blocks, b->d_rpartial, group_base[gi], b->d_rout, b->stream);
     if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("batched reduction: ") + cudaGetErrorString(e));
   }
   if (cudaMemcpyAsync(b->h_rout, b->d_rout, sizeof(double) * kRedMaxK * count, cudaMemcpyDeviceToHost, b->stream) !=
@@ -1258,6 +1260,114 @@ int32_t lbm_batch_reduce(lbm_batch* b, int32_t kind, const uint8_t* select, doub
     return bfail(b, LBM_ERR_CUDA, "batched reduction result");
   for (int k : order)
     for (int j = 0; j < K; ++j) out[(size_t)k * kRedMaxK + j] = b->h_rout[(size_t)k * kRedMaxK + j];
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// The reductions lbm_reduce computes without analytic fields (MEAN_VELOCITY,
+// VELOCITY_CONVERGENCE, CONSERVED) for the selected members at once: out[k * 16 + j] is what
+// lbm_reduce(member k, kind) would return in out[j].  One launch per velocity set plus one
+// fixed-order finish; VELOCITY_CONVERGENCE updates each member's previous-velocity planes as
+// lbm_reduce does.  CONSERVED reports the non-finite population count in out[k * 16 + 3].
+int32_t lbm_batch_reduce(lbm_batch* b, int32_t kind, const uint8_t* select, double* out) {
+  if (!b || !out) return LBM_ERR_INVALID;
+  if (kind != LBM_REDUCE_MEAN_VELOCITY && kind != LBM_REDUCE_VELOCITY_CONVERGENCE && kind != LBM_REDUCE_CONSERVED)
+    return bfail(b, LBM_ERR_UNSUPPORTED, "batched reductions: MEAN_VELOCITY, VELOCITY_CONVERGENCE, CONSERVED");
+  cudaSetDevice(b->device);
+  const int count = (int)b->members.size();
+  std::vector<int> selected;
+  for (int k = 0; k < count; ++k)
+    if (!select || select[k]) {
+      if (!b->members[k]->have_state) return bfail(b, LBM_ERR_STATE, "member without uploaded state");
+      selected.push_back(k);
+    }
+  int rc = batch_wait_members(b);
+  if (rc) return rc;
+  rc = batch_ensure_rargs(b);
+  if (rc) return rc;
+  rc = batch_reduce_run(b, red_kind_k(kind), selected, b->d_rargs, out);
+  if (rc) return rc;
+  return batch_release_members(b);
+}
+
+// The error-norm reductions with analytic fields (TRACK_ERRORS, COMPARE) for the selected
+// members at once; analytic[k] holds member k's host planes and scalars as lbm_reduce takes them.
+int32_t lbm_batch_reduce_fields(lbm_batch* b, int32_t kind, const uint8_t* select, const lbm_analytic* analytic,
+                                double* out) {
+  if (!b || !out || !analytic) return LBM_ERR_INVALID;
+  if (kind != LBM_REDUCE_TRACK_ERRORS && kind != LBM_REDUCE_COMPARE)
+    return bfail(b, LBM_ERR_UNSUPPORTED, "batched field reductions: TRACK_ERRORS, COMPARE");
+  cudaSetDevice(b->device);
+  const int count = (int)b->members.size();
+  const int need = kind == LBM_REDUCE_TRACK_ERRORS ? 8 : 4;
+  std::vector<int> selected;
+  size_t total = 0;
+  for (int k = 0; k < count; ++k) {
+    if (select && !select[k]) continue;
+    const lbm_analytic& an = analytic[k];
+    const double* src[8] = {an.rho, an.ux, an.uy, an.p, an.sxx, an.syx, an.sxy, an.syy};
+    if (!b->members[k]->have_state) return bfail(b, LBM_ERR_STATE, "member without uploaded state");
+    if (an.on_device) return bfail(b, LBM_ERR_UNSUPPORTED, "batched field reductions take host planes");
+    for (int j = 0; j < need; ++j)
+      if (!src[j]) return bfail(b, LBM_ERR_INVALID, "missing analytic field");
+    selected.push_back(k);
+    total += (size_t)need * b->members[k]->n;
+  }
+  int rc = batch_wait_members(b);
+  if (rc) return rc;
+  rc = batch_ensure_rargs(b);
+  if (rc) return rc;
+  if (total > b->ranal_cap) {
+    cudaFree(b->d_ranal);
+    if (b->h_ranal) cudaFreeHost(b->h_ranal);
+    b->d_ranal = nullptr;
+    b->h_ranal = nullptr;
+    b->ranal_cap = 0;
+    if (cudaMalloc((void**)&b->d_ranal, total * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_ranal, total * sizeof(double)) != cudaSuccess)
+      return bfail(b, LBM_ERR_NOMEM, "analytic staging");
+    b->ranal_cap = total;
+  }
+  if (!b->d_rargs_call && cudaMalloc((void**)&b->d_rargs_call, sizeof(ReduceArgs) * count) != cudaSuccess)
+    return bfail(b, LBM_ERR_NOMEM, "reduction arguments");
+  // pack the planes (the pinned staging is free: the previous call ended with a synchronize)
+  std::vector<ReduceArgs> args = b->h_rargs;
+  size_t off = 0;
+  for (int k : selected) {
+    const lbm_analytic& an = analytic[k];
+    const double* src[8] = {an.rho, an.ux, an.uy, an.p, an.sxx, an.syx, an.sxy, an.syy};
+    const size_t n = (size_t)b->members[k]->n;
+    const double* dp[8] = {};
+    for (int j = 0; j < need; ++j) {
+      std::memcpy(b->h_ranal + off, src[j], n * sizeof(double));
+      dp[j] = b->d_ranal + off;
+      off += n;
+    }
+    ReduceArgs& r = args[k];
+    r.rho_a = dp[0];
+    r.ux_a = dp[1];
+    r.uy_a = dp[2];
+    r.p_a = dp[3];
+    r.sxx_a = dp[4];
+    r.syx_a = dp[5];
+    r.sxy_a = dp[6];
+    r.syy_a = dp[7];
+    r.tau = an.tau;
+    r.u_max = an.u_max;
+    r.area = an.area;
+  }
+  if ((total && cudaMemcpyAsync(b->d_ranal, b->h_ranal, total * sizeof(double), cudaMemcpyHostToDevice, b->stream) !=
+                    cudaSuccess) ||
+      cudaMemcpyAsync(b->d_rargs_call, args.data(), sizeof(ReduceArgs) * count, cudaMemcpyHostToDevice, b->stream) !=
+          cudaSuccess)
+    return bfail(b, LBM_ERR_CUDA, "analytic upload");
+  rc = batch_reduce_run(b, red_kind_k(kind), selected, b->d_rargs_call, out);
+  // the pageable argument copy above completes before its call returns; the pinned planes
+  // were synchronised by the result read
+  if (rc) return rc;
   return batch_release_members(b);
 }
 

@@ -172,6 +172,14 @@ cudaError_t batch_reduce_s(int K, const void* statics, const ReduceArgs* args, c
       batch_reduce_kernel<L, S, 4><<<(unsigned)blocks, kRedThreads, 0, s>>>(m, args, dyn, nmem, part);
       batch_reduce_finish<4><<<fin_blocks, fin_threads, 0, s>>>(dyn, nmem, partial, part_base, out);
       break;
+    case 12:
+      batch_reduce_kernel<L, S, 12><<<(unsigned)blocks, kRedThreads, 0, s>>>(m, args, dyn, nmem, part);
+      batch_reduce_finish<12><<<fin_blocks, fin_threads, 0, s>>>(dyn, nmem, partial, part_base, out);
+      break;
+    case 16:
+      batch_reduce_kernel<L, S, 16><<<(unsigned)blocks, kRedThreads, 0, s>>>(m, args, dyn, nmem, part);
+      batch_reduce_finish<16><<<fin_blocks, fin_threads, 0, s>>>(dyn, nmem, partial, part_base, out);
+      break;
     default:
       return cudaErrorInvalidValue;
   }

@@ -172,7 +172,7 @@ class DeviceLattice:
 
     # ---- reductions --------------------------------------------------------------------
     def reduce(self, kind, fields=None, tau=0.0, u_max=1.0, area=0.0):
-        pre = self.prefetched.pop(kind, None) if fields is None else None
+        pre = self.prefetched.pop(kind, None)
         if pre is not None:  # computed for this lattice by a batched reduction (simulate_batch)
             return pre
         out = np.zeros(16)
@@ -272,6 +272,32 @@ class DeviceBatch:
         self._check(N.lib().lbm_batch_reduce(self.h, int(kind),
                                              sel.ctypes.data_as(C.POINTER(C.c_uint8)) if sel is not None else None,
                                              out.ctypes.data_as(N._DP)))
+        return out[:, : N.REDUCE_K[kind]]
+
+    def reduce_fields(self, kind, inputs):
+        """lbm_batch_reduce_fields: the TRACK_ERRORS / COMPARE sums of the members for which
+        `inputs[k]` = (fields dict of (NY, NX) host planes, tau, u_max, area) is given (None:
+        not selected); rows of unselected members are zero."""
+        n = len(self.lattices)
+        sel = np.zeros(n, dtype=np.uint8)
+        an = (N.LbmAnalytic * n)()
+        keep = []
+        for k, inp in enumerate(inputs):
+            if inp is None:
+                continue
+            fields, tau, u_max, area = inp
+            lat = self.lattices[k]
+            for name in ("rho", "ux", "uy", "p", "sxx", "syx", "sxy", "syy"):
+                a = fields.get(name)
+                if a is not None:
+                    a = _as_f64(a, (lat.ny, lat.nx))
+                    keep.append(a)
+                    setattr(an[k], name, a.ctypes.data_as(N._DP))
+            an[k].tau, an[k].u_max, an[k].area = float(tau), float(u_max), float(area)
+            sel[k] = 1
+        out = np.zeros((n, 16))
+        self._check(N.lib().lbm_batch_reduce_fields(self.h, int(kind), sel.ctypes.data_as(C.POINTER(C.c_uint8)), an,
+                                                    out.ctypes.data_as(N._DP)))
         return out[:, : N.REDUCE_K[kind]]
 
     def share_stream(self):

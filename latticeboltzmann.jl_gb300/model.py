@@ -223,7 +223,10 @@ def _simulate_batch_vectorised(models, pms, bounds, batch):
     for a stop criterion, and n_steps) and their stop decisions are computed for all members at
     once, and a member's own next!(model, t) is called only where it does more than decide not
     to stop (a row is due, or it stops); a MeanVelocity criterion that does not stop keeps its
-    new mean as next! would (stopping_criteria.jl:20-72)."""
+    new mean as next! would (stopping_criteria.jl:20-72).  The rows recorded in one round (the
+    error norms of every member that stops or reaches n_steps) come from one batched reduction."""
+    from .processing_methods import (CompareWithAnalyticalSolution, TrackHydrodynamicErrors, compare_inputs,
+                                     track_inputs)
     n = len(models)
     t = np.array([b[0] for b in bounds], dtype=np.int64)
     last = np.array([b[1] for b in bounds], dtype=np.int64)
@@ -269,6 +272,22 @@ def _simulate_batch_vectorised(models, pms, bounds, batch):
                     st = (conv < tol) | np.isnan(um)
             stop[sel] = st[sel]
         call = acting & (stop | (tact == nst))
+        # the rows these calls record: all members' error norms in one batched reduction per kind
+        idx = np.flatnonzero(call)
+        if idx.size:
+            for rkind, cls, make in ((N.REDUCE_TRACK_ERRORS, TrackHydrodynamicErrors, track_inputs),
+                                     (N.REDUCE_COMPARE, CompareWithAnalyticalSolution, compare_inputs)):
+                inputs = [None] * n
+                for k in idx:
+                    if type(pms[k]) is cls:
+                        pb = pms[k].problem
+                        tk = int(tact[k])
+                        inputs[k] = make(models[k], pb, tk if cls is TrackHydrodynamicErrors else tk * pb.delta_t())
+                if any(x is not None for x in inputs):
+                    rws = batch.reduce_fields(rkind, inputs)
+                    for k in idx:
+                        if inputs[k] is not None:
+                            models[k].lattice.prefetched[rkind] = rws[k]
         for k in np.flatnonzero(call):
             lat = models[k].lattice
             if due[k]:

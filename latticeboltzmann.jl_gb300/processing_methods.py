@@ -200,14 +200,22 @@ class TrackHydrodynamicErrors(ProcessingMethodBase):
         return should_stop
 
 
+def track_inputs(model, problem, t):
+    """The inputs of the TRACK_ERRORS reduction at step t: (analytic fields, tau, u_max, area)."""
+    q = model.quadrature
+    fields = analytic_fields(q, problem, t * problem.delta_t())
+    return fields, q.speed_of_sound_squared * problem.lattice_viscosity(), problem.u_max, 0.0
+
+
 def track_errors(model, problem, t):
     """One TrackHydrodynamicErrors row for the model's current state at step t
-    (track_hydrodynamic_errors.jl:68-221) from one device reduction."""
-    q = model.quadrature
-    time = t * problem.delta_t()
-    fields = analytic_fields(q, problem, time)
-    tau = q.speed_of_sound_squared * problem.lattice_viscosity()
-    s = model.lattice.reduce(N.REDUCE_TRACK_ERRORS, fields, tau=tau, u_max=problem.u_max)
+    (track_hydrodynamic_errors.jl:68-221) from one device reduction (or the sums a batched
+    reduction already supplied)."""
+    if N.REDUCE_TRACK_ERRORS in model.lattice.prefetched:
+        s = model.lattice.reduce(N.REDUCE_TRACK_ERRORS)
+    else:
+        fields, tau, u_max, _ = track_inputs(model, problem, t)
+        s = model.lattice.reduce(N.REDUCE_TRACK_ERRORS, fields, tau=tau, u_max=u_max)
     D_ = _mass_scale(problem, model.lattice.nx, model.lattice.ny)
     return TrackRow(int(t), _sqrt(s[0]), _sqrt(_div(s[1], s[7])), _sqrt(_div(s[2], s[12])),
                     _sqrt(_div(s[3], s[8])), _sqrt(_div(s[4], s[10])), _sqrt(_div(s[5], s[9])),
@@ -238,12 +246,19 @@ class CompareWithAnalyticalSolution(ProcessingMethodBase):
         return False
 
 
+def compare_inputs(model, problem, time):
+    """The inputs of the COMPARE reduction at physical time `time`: (fields, tau, u_max, area)."""
+    _, _, xs, ys = problem_range(problem)
+    return analytic_fields(model.quadrature, problem, time), 0.0, problem.u_max, ys * xs
+
+
 def compare_process(model, problem, time):
     """process!(problem, q, f, time, stats) (processing_methods.jl:142-269)."""
-    q = model.quadrature
-    fields = analytic_fields(q, problem, time)
-    _, _, xs, ys = problem_range(problem)
-    s = model.lattice.reduce(N.REDUCE_COMPARE, fields, u_max=problem.u_max, area=ys * xs)
+    if N.REDUCE_COMPARE in model.lattice.prefetched:
+        s = model.lattice.reduce(N.REDUCE_COMPARE)
+    else:
+        fields, _, u_max, area = compare_inputs(model, problem, time)
+        s = model.lattice.reduce(N.REDUCE_COMPARE, fields, u_max=u_max, area=area)
     return CompareRow(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9], _sqrt(s[10]), _sqrt(s[11]),
                       0.0, 0.0, 0.0, 0.0)
 

@@ -151,3 +151,33 @@ def test_batched_generic_path_every_step_processing(lbm_gpu):
         assert len(a) == len(b)
         for ra, rb in zip(a, b):
             np.testing.assert_array_equal(np.array(ra, dtype=float), np.array(rb, dtype=float))
+
+
+@pytest.mark.parametrize("storage", ["f64", "df64dev", "f32dev"])
+def test_batch_field_reductions_match_single_lattice(lbm_gpu, storage):
+    """lbm_batch_reduce_fields (TRACK_ERRORS, COMPARE with per-member analytic planes) gives
+    bitwise the sums lbm_reduce gives for each member."""
+    lbm = lbm_gpu
+    N = lbm._native
+    A = _lattices(lbm, storage)
+    batch = lbm.DeviceBatch([m.lattice for m in A])
+    batch.step(np.array([5, 2, 0], dtype=np.int64))
+    rng = np.random.default_rng(5)
+    inputs = []
+    for k, m in enumerate(A):
+        lat = m.lattice
+        fields = {name: rng.normal(size=(lat.ny, lat.nx)) * 1e-2 + (1.0 if name == "rho" else 0.0)
+                  for name in ("rho", "ux", "uy", "p", "sxx", "syx", "sxy", "syy")}
+        inputs.append(None if k == 1 else (fields, 0.3 + 0.1 * k, 0.05, 0.25))
+    for kind in (N.REDUCE_TRACK_ERRORS, N.REDUCE_COMPARE):
+        rows = batch.reduce_fields(kind, inputs)
+        for k, m in enumerate(A):
+            if inputs[k] is None:
+                assert not rows[k].any()
+                continue
+            fields, tau, u_max, area = inputs[k]
+            single = m.lattice.reduce(kind, fields, tau=tau, u_max=u_max, area=area)
+            np.testing.assert_array_equal(rows[k], single)
+    batch.close()
+    for m in A:
+        m.close()
