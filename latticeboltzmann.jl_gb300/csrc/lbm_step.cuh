@@ -18,12 +18,6 @@
 
 namespace lbm {
 
-template <class L, class S>
-struct Node {
-  using C = typename S::C;
-  C f[L::Q];
-};
-
 // Periodic pull offsets: xw[k] = (x - (k - R)) mod nx, yo[k] = ((y - (k - R)) mod ny) * nx.
 template <class L, class CT>
 __device__ __forceinline__ void pull_offsets(const StepParams<CT>& p, int x, int y, int* xw, int* yo) {
