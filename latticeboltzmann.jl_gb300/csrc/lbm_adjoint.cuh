@@ -41,9 +41,9 @@ __device__ __forceinline__ void adj_equilibrium(const StepParams<typename S::C>&
   using CT = typename S::C;
   const CT cs = p.cs;
   const CT usq = ux * ux + uy * uy;
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) {
-    const CT cxi = (CT)L::cx(i), cyi = (CT)L::cy(i);
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr CT cxi = (CT)L::cx(i), cyi = (CT)L::cy(i);
     const CT cu = cxi * ux + cyi * uy;
     const CT P2 = (CT)0.5 * (cs * cs * cu * cu - cs * usq);
     if constexpr (S::DEV) {
@@ -55,25 +55,28 @@ __device__ __forceinline__ void adj_equilibrium(const StepParams<typename S::C>&
       dfx[i] = rho * p.w[i] * (cs * cxi + cs * cs * cu * cxi - cs * ux);
       dfy[i] = rho * p.w[i] * (cs * cyi + cs * cs * cu * cyi - cs * uy);
     }
-  }
+  });
 }
 
+// Adds the block's sums of K values to its slots: every thread's values go to shared memory and
+// one warp adds them in a fixed order (a per-thread shuffle tree would cost 5 FP64 additions per
+// value and thread on a GPU that issues two FP64 instructions per SM per clock).
 template <int K>
 __device__ __forceinline__ void adj_block_add(double (&acc)[K], double* slots) {
-  __shared__ double sh[kAdjThreads / 32][K];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ double sh[K][kAdjThreads];
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double v = acc[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[warp][k] = v;
-  }
+  for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = acc[k];
   __syncthreads();
-  if (threadIdx.x < K) {
-    double s = 0.0;
-    for (int wi = 0; wi < kAdjThreads / 32; ++wi) s += sh[wi][threadIdx.x];
-    slots[(size_t)blockIdx.x * K + threadIdx.x] += s;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double v = sh[k][lane];
+      for (int j = lane + 32; j < kAdjThreads; j += 32) v += sh[k][j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) slots[(size_t)blockIdx.x * K + k] += v;
+    }
   }
 }
 
@@ -99,9 +102,10 @@ __global__ void __launch_bounds__(kAdjThreads) adj_loss_kernel(StepParams<typena
                                                                double* __restrict__ slots) {
   using CT = typename S::C;
   double acc[1] = {0.0};
-  for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
-       node += (long long)gridDim.x * kAdjThreads) {
-    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+  const long long first = (long long)blockIdx.x * kAdjThreads + threadIdx.x, stride = (long long)gridDim.x * kAdjThreads;
+  NodeWalk w(first, stride, p.nx);
+  for (long long node = first; node < p.n; node += stride, w.advance()) {
+    const int y = w.y, x = w.x;
     CT v[L::Q];
     load_streamed<L, S>(p, src, x, y, v);
     double rho = 0.0, jx = 0.0, jy = 0.0;
@@ -140,9 +144,10 @@ __global__ void __launch_bounds__(kAdjThreads, (S::DEV && L::Q <= 9) ? 4 : 1) ad
   const CT om_a = COLL == LBM_TRT ? p.inv_ta : p.om_b;
   const CT Fx = (CT)a.Fx, Fy = (CT)a.Fy, shift = (CT)a.shift;
   const CT sFx = (CT)(a.shift * a.Fx), sFy = (CT)(a.shift * a.Fy);
-  for (long long node = (long long)blockIdx.x * kAdjThreads + threadIdx.x; node < p.n;
-       node += (long long)gridDim.x * kAdjThreads) {
-    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
+  const long long first = (long long)blockIdx.x * kAdjThreads + threadIdx.x, stride = (long long)gridDim.x * kAdjThreads;
+  NodeWalk w(first, stride, p.nx);
+  for (long long node = first; node < p.n; node += stride, w.advance()) {
+    const int y = w.y, x = w.x;
     // forward state A_t at the node
     CT f[L::Q];
     if (pull) load_streamed<L, S>(p, src, x, y, f);
@@ -152,55 +157,56 @@ __global__ void __launch_bounds__(kAdjThreads, (S::DEV && L::Q <= 9) ? 4 : 1) ad
     {
       int xw[2 * L::R + 1], yo[2 * L::R + 1];
       pull_offsets<L>(p, x, y, xw, yo);
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        const int idx = yo[L::R - L::cy(i)] + xw[L::R - L::cx(i)];
-        mu[i] = (CT)lam_next[(size_t)i * p.n + idx];
-      }
+      static_for<0, L::Q>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        mu[i] = (CT)lam_next[(size_t)i * p.n + yo[L::R - L::cy(i)] + xw[L::R - L::cx(i)]];
+      });
     }
     // moments, equilibrium and its velocity derivatives (as the forward collision forms them)
     CT s = 0, jx = 0, jy = 0;
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
+    static_for<0, L::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
       s += f[i];
       jx += (CT)L::cx(i) * f[i];
       jy += (CT)L::cy(i) * f[i];
-    }
+    });
     const CT rho = S::DEV ? (CT)1 + s : s;
     const CT drho = s;
-    const CT ux = jx / rho, uy = jy / rho;
+    const CT inv_rho = (CT)1 / rho;
+    const CT ux = jx * inv_rho, uy = jy * inv_rho;
     const CT upx = ux + sFx, upy = uy + sFy;
     CT feq[L::Q], dfx[L::Q], dfy[L::Q];
     adj_equilibrium<L, S>(p, rho, drho, upx, upy, feq, dfx, dfy);
     // ν = N μ and M μ per opposite pair
     CT nu[L::Q], Mmu[L::Q];
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
-      const int o = L::opp(i);
+    static_for<0, L::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value, o = L::opp(i);
       const CT ms = (CT)0.5 * (mu[i] + mu[o]), ma = (CT)0.5 * (mu[i] - mu[o]);
       nu[i] = om_s * ms + om_a * ma;
       Mmu[i] = ((CT)1 - om_s) * ms + ((CT)1 - om_a) * ma;
       const CT fneq = f[i] - feq[i];  // deviation storage: g - geq
       tacc[0] -= ms * fneq;
       tacc[1] -= ma * fneq;
-    }
+    });
     CT Grho = 0, Gx = 0, Gy = 0;
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
+    static_for<0, L::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
       const CT fe = S::DEV ? feq[i] + p.w[i] : feq[i];
       Grho += nu[i] * fe;
       Gx += nu[i] * dfx[i];
       Gy += nu[i] * dfy[i];
-    }
-    Grho = Grho / rho;
+    });
+    Grho = Grho * inv_rho;
     tacc[2] += Gx * Fx + Gy * Fy;
     tacc[3] += shift * Gx;
     tacc[4] += shift * Gy;
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
-      const CT l = Mmu[i] + Grho + (Gx * ((CT)L::cx(i) - ux) + Gy * ((CT)L::cy(i) - uy)) / rho;
+    const CT gx = Gx * inv_rho, gy = Gy * inv_rho, base = Grho - (gx * ux + gy * uy);
+    static_for<0, L::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      constexpr CT cxi = (CT)L::cx(i), cyi = (CT)L::cy(i);
+      const CT l = Mmu[i] + base + (gx * cxi + gy * cyi);
       lam_out[(size_t)i * p.n + node] = (typename S::T)l;
-    }
+    });
   }
   double acc[kAdjParams];
 #pragma unroll

@@ -75,8 +75,8 @@ __global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchStatic<t
   const StepParams<typename S::C>& p = m.p;
   const long long node = (b - d.block_start) * kBlockX + threadIdx.x;
   if (node >= p.n) return;
-  const int y = (int)(node / p.nx);
-  const int x = (int)(node - (long long)y * p.nx);
+  const int y = (int)node / p.nx;
+  const int x = (int)node - y * p.nx;
   const int parity = (int)((d.cur0 + t) & 1);
   const T* src = static_cast<const T*>(parity ? m.buf1 : m.buf0);
   T* dst = static_cast<T*>(parity ? m.buf0 : m.buf1);
@@ -104,10 +104,10 @@ __global__ void __launch_bounds__(kRedThreads) batch_reduce_kernel(const BatchSt
   for (int k = 0; k < K; ++k) acc[k] = 0.0;
   const long long first = (b - d.block_start) * kRedThreads + threadIdx.x;
   const long long stride = d.steps * kRedThreads;
-  for (long long node = first; node < m.p.n; node += stride) {
-    const int y = (int)(node / m.p.nx), x = (int)(node - (long long)y * m.p.nx);
-    if (d.phase0) reduce_node<L, S, true, K>(m.p, r, src, x, y, node, acc);
-    else reduce_node<L, S, false, K>(m.p, r, src, x, y, node, acc);
+  NodeWalk w(first, stride, m.p.nx);
+  for (long long node = first; node < m.p.n; node += stride, w.advance()) {
+    if (d.phase0) reduce_node<L, S, true, K>(m.p, r, src, w.x, w.y, node, acc);
+    else reduce_node<L, S, false, K>(m.p, r, src, w.x, w.y, node, acc);
   }
   block_reduce_store<K>(acc, partial);
 }

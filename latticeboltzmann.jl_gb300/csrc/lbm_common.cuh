@@ -25,6 +25,28 @@ __device__ __forceinline__ void static_for(F&& f) {
   }
 }
 
+// Coordinates (x fastest) of the node numbers first, first + stride, ... of a grid-stride loop,
+// with one 32-bit division at the start instead of a 64-bit division per node (lattices have
+// fewer than 2^31 nodes, and strides are a grid's thread count).
+struct NodeWalk {
+  int x, y, sx, sy, nx;
+  __device__ __forceinline__ NodeWalk(long long first, long long stride, int nx_) : nx(nx_) {
+    const int n0 = (int)first, st = (int)stride;
+    y = n0 / nx;
+    x = n0 - y * nx;
+    sy = st / nx;
+    sx = st - sy * nx;
+  }
+  __device__ __forceinline__ void advance() {
+    x += sx;
+    y += sy;
+    if (x >= nx) {
+      x -= nx;
+      ++y;
+    }
+  }
+};
+
 // Additions inside sums whose result feeds further arithmetic: plain for FP32 / FP64; for
 // float-float without the closing renormalisation (add_lazy, lbm_df64.cuh).
 template <class CT>

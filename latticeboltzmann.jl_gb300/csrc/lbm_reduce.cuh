@@ -176,11 +176,10 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(StepParams<typename
   double acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = 0.0;
-  for (long long node = (long long)blockIdx.x * kRedThreads + threadIdx.x; node < p.n;
-       node += (long long)gridDim.x * kRedThreads) {
-    const int y = (int)(node / p.nx), x = (int)(node - (long long)y * p.nx);
-    reduce_node<L, S, PULL, K>(p, r, src, x, y, node, acc);
-  }
+  const long long first = (long long)blockIdx.x * kRedThreads + threadIdx.x, stride = (long long)gridDim.x * kRedThreads;
+  NodeWalk w(first, stride, p.nx);
+  for (long long node = first; node < p.n; node += stride, w.advance())
+    reduce_node<L, S, PULL, K>(p, r, src, w.x, w.y, node, acc);
   block_reduce_store<K>(acc, partial);
 }
 
