@@ -298,6 +298,41 @@ __device__ __forceinline__ void mrt_out_pair(const StepParams<CT>& p, const MrtC
   out_o = we - wo;
 }
 
+// Index of the velocity (cx, cy) in set L, or -1.
+template <class L>
+__host__ __device__ constexpr int vel_index(int cx, int cy) {
+  for (int j = 0; j < L::Q; ++j)
+    if (L::cx(j) == cx && L::cy(j) == cy) return j;
+  return -1;
+}
+
+// Velocity i with both components positive heads the quadruple {(a, b), (a, -b), (-a, b), (-a, -b)}.
+template <class L>
+__host__ __device__ constexpr bool quad_head(int i) {
+  return L::cx(i) > 0 && L::cy(i) > 0 && vel_index<L>(L::cx(i), -L::cy(i)) >= 0 &&
+         vel_index<L>(-L::cx(i), L::cy(i)) >= 0;
+}
+template <class L>
+__host__ __device__ constexpr bool in_quad(int i) {
+  const int a = L::cx(i) < 0 ? -L::cx(i) : L::cx(i), b = L::cy(i) < 0 ? -L::cy(i) : L::cy(i);
+  return a > 0 && b > 0 && quad_head<L>(vel_index<L>(a, b));
+}
+
+// Raw moments of one quadruple: with u1 = f(a,b) + f(-a,-b), u2 = f(a,b) - f(-a,-b),
+// u3 = f(a,-b) + f(-a,b), u4 = f(a,-b) - f(-a,b), a moment M_kl gains a^k b^l times
+// u1 + u3 (k, l even), u1 - u3 (both odd), u2 - u4 (k even, l odd) or u2 + u4 (k odd, l even).
+template <class L, int I, class CT>
+__device__ __forceinline__ void mrt_accumulate_quad(CT* M, bool* set, CT fpp, CT fpm, CT fmp, CT fmm) {
+  const CT u1 = ladd(fpp, fmm), u2 = lsub(fpp, fmm), u3 = ladd(fpm, fmp), u4 = lsub(fpm, fmp);
+  const CT ee = ladd(u1, u3), oo = lsub(u1, u3), eo = lsub(u2, u4), oe = ladd(u2, u4);
+  static_for<0, mom_count(L::HN)>([&](auto K) {
+    constexpr int k = decltype(K)::value, ka = mom_a(k), kb = mom_b(k);
+    constexpr int coef = ipow(L::cx(I), ka) * ipow(L::cy(I), kb);
+    const CT& e = (ka & 1) ? ((kb & 1) ? oo : oe) : ((kb & 1) ? eo : ee);
+    acc_add<coef>(M[k], set[k], e);
+  });
+}
+
 // Regularised MRT collision on one node (mrt.jl:135-197), written with raw moments: the
 // Hermite coefficients a_f^(n) = Σ f_i H_n(c_i) of orders 2..N are formed from the raw
 // moments M_ab, relaxed towards a_eq^(n) = ρ u^{⊗n}, and the populations are rebuilt as
@@ -305,6 +340,8 @@ __device__ __forceinline__ void mrt_out_pair(const StepParams<CT>& p, const MrtC
 // DEV: v holds g = f - w and receives g_out = f_out - w.  The weights' own Hermite moments
 // of orders 1..N vanish (the quadrature symmetry the reference tests, test/quadrature.jl:1-19),
 // so the coefficients of f equal those formed from g, with ρ - 1 in place of ρ where M_00 enters.
+// Velocities off the axes are taken four at a time, {(±a, ±b)}, through their parity
+// combinations (one term per moment for the four), axis velocities in opposite pairs.
 // `pop(std::integral_constant<int, i>)` supplies population i; `out(i, value)` receives it.
 template <class L, bool DEV, class CT, class Pop, class Out>
 __device__ __forceinline__ void mrt_node(const StepParams<CT>& p, CT sFx, CT sFy, bool has_force, Pop&& pop,
@@ -317,9 +354,13 @@ __device__ __forceinline__ void mrt_node(const StepParams<CT>& p, CT sFx, CT sFy
     constexpr int i = decltype(I)::value, o = L::opp(i);
     if constexpr (o == i) {
       acc_add<1>(M[0], ms[0], pop(I));
-    } else if constexpr (o > i) {
+    } else if constexpr (quad_head<L>(i)) {
+      constexpr int ipm = vel_index<L>(L::cx(i), -L::cy(i)), imp = vel_index<L>(-L::cx(i), L::cy(i));
+      mrt_accumulate_quad<L, i>(M, ms, pop(I), pop(std::integral_constant<int, ipm>{}),
+                                pop(std::integral_constant<int, imp>{}), pop(std::integral_constant<int, o>{}));
+    } else if constexpr (!in_quad<L>(i) && o > i) {
       const CT a = pop(I), b = pop(std::integral_constant<int, o>{});
-      mrt_accumulate_pair<L, i>(M, ms, a + b, a - b);
+      mrt_accumulate_pair<L, i>(M, ms, ladd(a, b), lsub(a, b));
     }
   });
   static_for<0, NM>([&](auto K) {
@@ -332,7 +373,33 @@ __device__ __forceinline__ void mrt_node(const StepParams<CT>& p, CT sFx, CT sFy
     constexpr int i = decltype(I)::value, o = L::opp(i);
     if constexpr (o == i) {
       out(i, p.w[i] * c.B[0]);
-    } else if constexpr (o > i) {
+    } else if constexpr (quad_head<L>(i)) {
+      // parity sums P_ee, P_eo, P_oe, P_oo of the monomials at (a, b); the four outputs are their
+      // signed combinations (first-order terms with w1 in deviation storage)
+      constexpr int ipm = vel_index<L>(L::cx(i), -L::cy(i)), imp = vel_index<L>(-L::cx(i), L::cy(i));
+      CT P[4];  // ee, eo, oe, oo
+      bool ps[4] = {true, false, false, false};
+      P[0] = c.B[0];
+      static_for<(DEV ? 3 : 1), NM>([&](auto K) {
+        constexpr int k = decltype(K)::value, ka = mom_a(k), kb = mom_b(k);
+        constexpr int coef = ipow(L::cx(i), ka) * ipow(L::cy(i), kb);
+        constexpr int slot = ((ka & 1) ? 2 : 0) + ((kb & 1) ? 1 : 0);
+        acc_add<coef>(P[slot], ps[slot], c.B[k]);
+      });
+      const CT w = p.w[i];
+      const CT Tee = w * P[0];
+      CT Teo = ps[1] ? w * P[1] : (CT)0, Toe = ps[2] ? w * P[2] : (CT)0;
+      const CT Too = ps[3] ? w * P[3] : (CT)0;
+      if constexpr (DEV) {
+        Teo = ladd(Teo, p.w1[i] * ((CT)L::cy(i) * c.B2p));
+        Toe = ladd(Toe, p.w1[i] * ((CT)L::cx(i) * c.B1p));
+      }
+      const CT v1 = ladd(Tee, Too), v2 = lsub(Tee, Too), v3 = ladd(Teo, Toe), v4 = lsub(Toe, Teo);
+      out(i, v1 + v3);
+      out(o, v1 - v3);
+      out(ipm, v2 + v4);
+      out(imp, v2 - v4);
+    } else if constexpr (!in_quad<L>(i) && o > i) {
       CT a, b;
       mrt_out_pair<L, DEV, i>(p, c, a, b);
       out(i, a);
