@@ -266,7 +266,7 @@ def bench_all_sets(torch, lbm, n=2048, steps=40):
     for qn in ("D2Q4", "D2Q5", "D2Q9", "D2Q13", "D2Q17", "D2Q21", "D2Q37"):
         q = lbm.Quadratures[qn]
         row = {}
-        for storage, esize in (("f64", 8), ("df64dev", 8), ("f32dev", 4)):
+        for storage, esize in (("f64", 8), ("df64dev", 8), ("f32dev", 4), ("f16dev", 2)):
             lat = lbm.DeviceLattice(q, n, n, lbm.TRT.fields(0.8, 1.1), (), force=("constant", (1e-6, 0.0)),
                                     storage=storage)
             lat.initialize_fields()
