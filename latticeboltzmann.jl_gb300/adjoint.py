@@ -18,7 +18,6 @@ import math
 import numpy as np
 
 from . import _native as N
-from .collision_models import SRT, TRT
 from .device import DeviceLattice
 
 

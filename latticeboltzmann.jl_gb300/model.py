@@ -12,7 +12,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _native as N
-from .collision_models import (IterativeInitializationCollisionModel, MRT, SRT, TRT, make_collision_model)
+from .collision_models import IterativeInitializationCollisionModel, SRT, make_collision_model
 from .device import DeviceLattice
 from .initial_conditions import default_strategy, initial_fields, initialize
 from .problems import DecayingShearFlow, PoiseuilleFlow, CouetteFlow, lattice_force_field, problem_range

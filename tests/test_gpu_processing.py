@@ -1,7 +1,6 @@
 """The simulate loop with the reference's processing methods, on the device, against the
 oracle and against the reference's own printed results."""
 import json
-import math
 import os
 
 import numpy as np
