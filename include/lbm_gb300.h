@@ -227,7 +227,7 @@ int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old); 
  * still running.  Members keep their buffers; upload / download / reduce them as usual before
  * and after (their streams are ordered against the batch). */
 typedef struct lbm_batch lbm_batch;
-int32_t lbm_batch_create(lbm_batch** batch, lbm_ctx* const* members, int32_t count);
+int32_t lbm_batch_create(lbm_batch** batch, lbm_ctx* const* members, int32_t count);  /* each context at most once */
 void lbm_batch_destroy(lbm_batch* batch);
 int32_t lbm_batch_step(lbm_batch* batch, const int64_t* nsteps);
 int32_t lbm_batch_set_stream(lbm_batch* batch, void* stream);

@@ -984,6 +984,11 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
     if (c->storage == LBM_STORE_F16_DEV) return LBM_ERR_UNSUPPORTED;
     if (c->force_kind == LBM_FORCE_SHEAR) return LBM_ERR_UNSUPPORTED;  // time-dependent forces
   }
+  {  // a context may appear once: the batch advances each member's own buffers
+    std::vector<lbm_ctx*> sorted(members, members + count);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return LBM_ERR_INVALID;
+  }
   lbm_batch* b = new lbm_batch();
   b->members.assign(members, members + count);
   b->device = c0->device;

@@ -63,6 +63,8 @@ def test_unsupported_combinations(lbm_gpu):
     c = _lattice(lbm, cm=lbm.SRT(0.8))
     with pytest.raises(N.LbmError):            # ... and the collision kind
         lbm.DeviceBatch([a, c])
+    with pytest.raises(N.LbmError):            # ... and appear once
+        lbm.DeviceBatch([a, a])
     h = C.c_void_p()
     d17 = _lattice(lbm, "D2Q17")
     assert L.lbm_adjoint_create(C.byref(h), d17.h, 10, 0) == N.LBM_ERR_UNSUPPORTED
