@@ -146,3 +146,35 @@ def test_autograd_function_returns_the_adjoint_gradients(lbm_gpu):
     with torch.no_grad():
         u_step = u - 1e-3 * u.grad / u.grad.abs().max()
     assert float(lbm.LBMLoss.apply(u_step, tau, F, factory, ut).detach()) < float(loss.detach())
+
+
+@pytest.mark.parametrize("qname,coll", [("D2Q13", "TRT"), ("D2Q9", "SRT"), ("D2Q13", "SRT")])
+def test_other_sets_and_srt_match_finite_differences(lbm_gpu, qname, coll):
+    """The adjoint of D2Q13 and of SRT (one relaxation time): ∂L/∂τ and ∂L/∂F_x against
+    fourth-order central differences of the device forward model."""
+    lbm = lbm_gpu
+    q = lbm.Quadratures[qname]
+    n, steps = 24, 60
+    u0 = lbm.divergence_free_field(n, n, kmax=3, amplitude=0.01, seed=3)
+    ut = lbm.divergence_free_field(n, n, kmax=3, amplitude=0.01, seed=4)
+
+    def cm(tau):
+        return lbm.SRT(tau) if coll == "SRT" else lbm.TRT.fields(tau, 1.1)
+
+    def loss(tau, F):
+        p = lbm.AdjointProblem(q, n, n, cm(tau), force=F, nsteps=steps)
+        L = p.loss(u0, ut)
+        p.close()
+        return L
+
+    def fd(fun, h):
+        return (fun(-2 * h) - 8 * fun(-h) + 8 * fun(h) - fun(2 * h)) / (12 * h)
+
+    tau, F = 0.85, (3e-6, 1e-6)
+    p = lbm.AdjointProblem(q, n, n, cm(tau), force=F, nsteps=steps)
+    res = p.run(u0, ut)
+    p.close()
+    fd_tau = fd(lambda e: loss(tau + e, F), 1e-4)
+    fd_fx = fd(lambda e: loss(tau, (F[0] + e, F[1])), 1e-7)
+    assert res["dtau_s"] == pytest.approx(fd_tau, rel=1e-6, abs=1e-12)
+    assert res["dF"][0] == pytest.approx(fd_fx, rel=1e-6, abs=1e-12)
