@@ -87,3 +87,33 @@ def test_couette_is_exact(lbm_gpu):
     for m in models:
         m.close()
     assert all(e < 1e-9 for e in err), err
+
+
+@pytest.mark.parametrize("storage", ["f64", "df64dev"])
+@pytest.mark.parametrize("qname,coll,tau,expected", [
+    ("D2Q9", "SRT", 0.8, [0.01025303463523784, 0.0025634013437757994, 0.0006408694124712757]),
+    ("D2Q37", "MRT", 0.6, [0.031105040526872192, 0.007620077764117277, 0.0018956208479634419]),
+])
+def test_shear_wave_decay_second_order(lbm_gpu, storage, qname, coll, tau, expected):
+    """Shear-wave decay u_x = u0 sin(2π y / N) exp(-ν k² t) (the D2Q37 regularised-MRT
+    configuration's flow) over N = 16, 32, 64 with N²/16 steps, one batch: error_u equals the
+    oracle's rows and falls with second order."""
+    lbm = lbm_gpu
+    q = lbm.Quadratures[qname]
+    nu = (tau - 0.5) / q.speed_of_sound_squared
+    sizes = [16, 32, 64]
+    models, times = [], []
+    for n in sizes:
+        problem = lbm.ShearWave(n, n, nu, 0.01)
+        steps = n * n // 16
+        pm = lbm.TrackHydrodynamicErrors(problem, False, steps)
+        cm = lbm.SRT(tau) if coll == "SRT" else lbm.MRT(q, tau)
+        models.append(lbm.LatticeBoltzmannModel(problem, q, collision_model=cm, process_method=pm, storage=storage,
+                                                initialization_strategy=lbm.AnalyticalEquilibrium()))
+        times.append(range(0, steps))
+    lbm.simulate_batch(models, times)
+    err = [m.processing_method.df[-1].error_u for m in models]
+    for m in models:
+        m.close()
+    assert err == pytest.approx(expected, rel=1e-9)
+    assert 1.9 < _order(sizes, err) < 2.1
