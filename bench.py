@@ -232,11 +232,14 @@ def bench_mrt_d2q37(torch, lbm, steps=500, n=2048):
 
 
 def bench_batched(torch, lbm):
-    res = lbm.run_tgv_study(storage="df64dev", torch=torch)
-    res.pop("errors", None)
-    res["workload"] = ("48 Taylor-Green lattices N in {16..1024}^2 x {D2Q9, D2Q17}, tau ~ U[0.51, 2.0] (seeded), "
-                       "steps = N^2/256, float-float storage, one CUDA graph vs one lattice after another")
-    return res
+    """The convergence study in FP64 (the study's own precision) and in float-float storage."""
+    out = {"workload": ("48 Taylor-Green lattices N in {16..1024}^2 x {D2Q9, D2Q17}, tau ~ U[0.51, 2.0] (seeded), "
+                        "steps = N^2/256, one CUDA graph vs one lattice after another; FP64 and float-float storage")}
+    for storage in ("f64", "df64dev"):
+        res = lbm.run_tgv_study(storage=storage, torch=torch)
+        res.pop("errors", None)
+        out[storage] = res
+    return out
 
 
 def bench_trt_sweep(torch, lbm, every=40):

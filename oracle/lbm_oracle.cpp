@@ -152,6 +152,27 @@ static int opposite(const Quad& q, int j) {
 // ---------------------------------------------------------------------------------------
 static inline int dlt(int a, int b) { return a == b ? 1 : 0; }
 
+// Forward-mode dual number v + d ε (ε² = 0).  Instantiating the equilibrium, moment, SRT/TRT
+// collision and stream templates below with it carries one directional derivative alongside
+// every value: the forward-mode stand-in for ForwardDiff through the reference loop (the
+// reference itself cannot take dual numbers: srt.jl:2 types τ as Float64).  The value part
+// repeats the double arithmetic operation for operation, so it equals the double loop bitwise.
+struct Dual {
+  double v = 0.0, d = 0.0;
+  Dual() = default;
+  Dual(double a) : v(a) {}
+  Dual(double a, double b) : v(a), d(b) {}
+};
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b) {
+  const double q = a.v / b.v;
+  return {q, (a.d - q * b.d) / b.v};
+}
+inline Dual& operator+=(Dual& a, Dual b) { return a = a + b; }
+
 // hermite(Val{n}, ξ, q): src/hermite_polynomials.jl:47-82.  Tensors are flattened
 // column-major (first index fastest), 2^n entries.  cs = 1 / q.speed_of_sound_squared.
 static void hermite_q(int n, const int* xi, double cs, double* H) {
@@ -258,14 +279,15 @@ static void hermite_equilibrium(const Quad& q, double rho, const double* u, doub
 //   third order for D2Q17 / D2Q21   velocity_distribution_function/quadratures.jl:3-19,45-61
 //   fourth order for D2Q37          velocity_distribution_function/quadratures.jl:63-124
 //   first order for D2Q4 / D2Q5     velocity_distribution_function/quadratures.jl:129-159
-static void equilibrium(const Quad& q, double rho, const double* u, double* f) {
-  double u_squared = 0.0;
+template <class R>
+static void equilibrium(const Quad& q, R rho, const R* u, R* f) {
+  R u_squared = 0.0;
   for (int d = 0; d < 2; ++d) u_squared += u[d] * u[d];
   const double cs = q.cs;
   for (int i = 0; i < q.Q; ++i) {
-    const double cu = q.cx[i] * u[0] + q.cy[i] * u[1];
-    const double rw = rho * q.w[i];
-    const double a1 = cs * cu;
+    const R cu = q.cx[i] * u[0] + q.cy[i] * u[1];
+    const R rw = rho * q.w[i];
+    const R a1 = cs * cu;
     switch (q.id) {
       case Q_D2Q4:
       case Q_D2Q5:
@@ -273,24 +295,24 @@ static void equilibrium(const Quad& q, double rho, const double* u, double* f) {
         break;
       case Q_D2Q9:
       case Q_D2Q13: {
-        const double a2 = ((cs * cs) * (cu * cu) + 0.0) + (-cs * u_squared);
+        const R a2 = ((cs * cs) * (cu * cu) + 0.0) + (-cs * u_squared);
         f[i] = rw * ((1.0 + a1) + 0.5 * a2);
         break;
       }
       case Q_D2Q17:
       case Q_D2Q21: {
-        const double a2 = ((cs * cs) * (cu * cu) + 0.0) + (-cs * u_squared);
-        const double a3 = (cs * cu) * (((cs * cs) * (cu * cu) - (3.0 * cs) * u_squared) + 0.0);
+        const R a2 = ((cs * cs) * (cu * cu) + 0.0) + (-cs * u_squared);
+        const R a3 = (cs * cu) * (((cs * cs) * (cu * cu) - (3.0 * cs) * u_squared) + 0.0);
         f[i] = rw * (((1.0 + a1) + 0.5 * a2) + (1.0 / 6.0) * a3);
         break;
       }
       case Q_D2Q37: {
-        const double a2 = ((cs * cs) * (cu * cu) + 0.0) + (-cs * u_squared);
-        const double a3 = (cs * cu) * (((cs * cs) * (cu * cu) - (3.0 * cs) * u_squared) + 0.0);
+        const R a2 = ((cs * cs) * (cu * cu) + 0.0) + (-cs * u_squared);
+        const R a3 = (cs * cu) * (((cs * cs) * (cu * cu) - (3.0 * cs) * u_squared) + 0.0);
         const double cs2 = cs * cs, cs3 = cs2 * cs, cs4 = cs2 * cs2;
-        const double cu2 = cu * cu;
-        const double a4 = (cs4 * (cu2 * cu2) - ((6.0 * cs3) * u_squared) * cu2) +
-                          (3.0 * cs2) * (u_squared * u_squared);
+        const R cu2 = cu * cu;
+        const R a4 = (cs4 * (cu2 * cu2) - ((6.0 * cs3) * u_squared) * cu2) +
+                     (3.0 * cs2) * (u_squared * u_squared);
         f[i] = rw * ((((1.0 + a1) + 0.5 * a2) + (1.0 / 6.0) * a3) + (1.0 / 24.0) * a4);
         break;
       }
@@ -299,14 +321,16 @@ static void equilibrium(const Quad& q, double rho, const double* u, double* f) {
 }
 
 // density / velocity!: src/velocity_distribution_function/moments.jl:1-19
-static double density(const Quad& q, const double* f) {
-  double s = f[0];
+template <class R>
+static R density(const Quad& q, const R* f) {
+  R s = f[0];
   for (int i = 1; i < q.Q; ++i) s += f[i];
   return s;
 }
-static void velocity(const Quad& q, const double* f, double rho, double* u) {
+template <class R>
+static void velocity(const Quad& q, const R* f, R rho, R* u) {
   for (int d = 0; d < 2; ++d) {
-    double s = 0.0;
+    R s = 0.0;
     const int* c = d == 0 ? q.cx : q.cy;
     for (int i = 0; i < q.Q; ++i) s += f[i] * c[i];
     u[d] = s / rho;
@@ -696,6 +720,39 @@ static Vec2 lattice_force(const Model& m, int xi, int yi, double t) {
   return {s * F.x, s * F.y};
 }
 
+// One node of collide! for SRT (srt.jl:18-62, kind 0, τ = tau0) and TRT (trt.jl:42-97,
+// kind 1, τ_s = tau0, τ_a = tau1): f holds the node's Q populations, (Fx, Fy) its lattice force
+// (added to u times τ, resp. τ_a, when `force`), out receives the post-collision populations.
+template <class R>
+static void collide_srt_trt_node(const Quad& q, int kind, R tau0, R tau1, bool force, R Fx, R Fy, const R* f,
+                                 R* out) {
+  const int Q = q.Q;
+  const R rho = density(q, f);
+  R u[2], feq[37];
+  velocity(q, f, rho, u);
+  const R shift = kind == 0 ? tau0 : tau1;
+  if (force) {
+    const R us[2] = {u[0] + shift * Fx, u[1] + shift * Fy};
+    equilibrium(q, rho, us, feq);
+  } else {
+    equilibrium(q, rho, (const R*)u, feq);
+  }
+  if (kind == 0) {
+    const R tau = tau0;
+    for (int i = 0; i < Q; ++i) out[i] = (1 - 1 / tau) * f[i] + (1 / tau) * feq[i];
+  } else {
+    const R ts = tau0, ta = tau1;
+    for (int i = 0; i < Q; ++i) {
+      const int o = opposite(q, i);
+      const R feq_s = 0.5 * (feq[i] + feq[o]);
+      const R feq_a = 0.5 * (feq[i] - feq[o]);
+      const R f_s = 0.5 * (f[i] + f[o]);
+      const R f_a = 0.5 * (f[i] - f[o]);
+      out[i] = f[i] + (-(1 / ts) * (f_s - feq_s) - (1 / ta) * (f_a - feq_a));
+    }
+  }
+}
+
 // collide! for SRT (srt.jl:18-62), TRT (trt.jl:42-97), MRT (mrt.jl:49-118), and the
 // iterative-initialisation model (iterative_initialization.jl:41-60).  Loop order x outer,
 // y inner, as in the reference.
@@ -716,40 +773,24 @@ static void collide(Model& m, const std::vector<double>& fin, std::vector<double
       }
 #pragma omp parallel for schedule(static) num_threads(m.nthreads) if (m.nthreads > 1)
   for (int x = 0; x < nx; ++x) {
-    double f[37], feq[37];
+    double f[37];
     for (int y = 0; y < ny; ++y) {
       for (int i = 0; i < Q; ++i) f[i] = fin[m.idx(x, y, i)];
+      if (cm.kind == 0 || cm.kind == 1) {  // SRT, TRT
+        double Fx = 0.0, Fy = 0.0, out[37];
+        if (cm.force_kind) {
+          const Vec2 F = lattice_force(m, x, y, time);
+          Fx = F.x;
+          Fy = F.y;
+        }
+        collide_srt_trt_node<double>(q, cm.kind, cm.tau[0], cm.tau[1], cm.force_kind != 0, Fx, Fy, f, out);
+        for (int i = 0; i < Q; ++i) fout[m.idx(x, y, i)] = out[i];
+        continue;
+      }
       const double rho = density(q, f);
       double u[2];
       velocity(q, f, rho, u);
-      if (cm.kind == 0) {  // SRT
-        const double tau = cm.tau[0];
-        if (cm.force_kind) {
-          const Vec2 F = lattice_force(m, x, y, time);
-          const double us[2] = {u[0] + tau * F.x, u[1] + tau * F.y};
-          equilibrium(q, rho, us, feq);
-        } else {
-          equilibrium(q, rho, u, feq);
-        }
-        for (int i = 0; i < Q; ++i) fout[m.idx(x, y, i)] = (1 - 1 / tau) * f[i] + (1 / tau) * feq[i];
-      } else if (cm.kind == 1) {  // TRT
-        const double ts = cm.tau[0], ta = cm.tau[1];
-        if (cm.force_kind) {
-          const Vec2 F = lattice_force(m, x, y, time);
-          const double us[2] = {u[0] + ta * F.x, u[1] + ta * F.y};
-          equilibrium(q, rho, us, feq);
-        } else {
-          equilibrium(q, rho, u, feq);
-        }
-        for (int i = 0; i < Q; ++i) {
-          const int o = opposite(q, i);
-          const double feq_s = 0.5 * (feq[i] + feq[o]);
-          const double feq_a = 0.5 * (feq[i] - feq[o]);
-          const double f_s = 0.5 * (f[i] + f[o]);
-          const double f_a = 0.5 * (f[i] - f[o]);
-          fout[m.idx(x, y, i)] = f[i] + (-(1 / ts) * (f_s - feq_s) - (1 / ta) * (f_a - feq_a));
-        }
-      } else if (cm.kind == 2) {  // MRT (regularised / projected)
+      if (cm.kind == 2) {  // MRT (regularised / projected)
         const double cs = q.cs;
         if (cm.force_kind) {
           const Vec2 F = lattice_force(m, x, y, time);
@@ -796,16 +837,19 @@ static inline int mod1(int a, int n) {  // Julia mod1 for positive n, 1-based re
 }
 
 // stream!: periodic pull, stream.jl:18-30,69-74
-static void stream(Model& m, const std::vector<double>& f, std::vector<double>& fnew) {
-  const Quad& q = m.q;
-  const int nx = m.nx, ny = m.ny;
-#pragma omp parallel for schedule(static) num_threads(m.nthreads) if (m.nthreads > 1)
+template <class R>
+static void stream_periodic(const Quad& q, int nx, int ny, const R* f, R* fnew, int nthreads) {
+  auto idx = [&](int x, int y, int i) { return (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * i); };
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
   for (int x = 1; x <= nx; ++x)
     for (int y = 1; y <= ny; ++y)
       for (int i = 0; i < q.Q; ++i) {
         const int fx = mod1(x - q.cx[i], nx), fy = mod1(y - q.cy[i], ny);
-        fnew[m.idx(x - 1, y - 1, i)] = f[m.idx(fx - 1, fy - 1, i)];
+        fnew[idx(x - 1, y - 1, i)] = f[idx(fx - 1, fy - 1, i)];
       }
+}
+static void stream(Model& m, const std::vector<double>& f, std::vector<double>& fnew) {
+  stream_periodic(m.q, m.nx, m.ny, f.data(), fnew.data(), m.nthreads);
 }
 
 // apply!(bcs, q, f_new, f_old): boundary_conditions.jl:6-20 in list order;
@@ -973,7 +1017,7 @@ int orc_initialize(int strategy, int qid, const orc_problem* p, double* f) {
   for (int x = 0; x < nx; ++x)
     for (int y = 0; y < ny; ++y) {
       const double X = xr[x], Y = yr[y];
-      double fl[37];
+      double fl[37] = {0};
       if (strategy == 0) {  // initial_conditions.jl:44-53
         for (int i = 0; i < Q; ++i) fl[i] = q.w[i];
       } else if (strategy == 1 || strategy == 2) {
@@ -1121,7 +1165,7 @@ static void track_errors(const Model& m, const std::vector<double>& f, long t, d
       tsxy += es.m[2] * es.m[2];
       tsyx += es.m[1] * es.m[1];
       tp2 += ep * ep;
-      double fl[37];
+      double fl[37] = {0};
       for (int i = 0; i < q.Q; ++i) fl[i] = f[m.idx(x, y, i)];
       const double rho = density(q, fl);
       double u[2];
@@ -1186,7 +1230,7 @@ static void compare_process(const Model& m, const std::vector<double>& f, double
   double eu = 0, ep = 0;
   for (int x = 0; x < m.nx; ++x)
     for (int y = 0; y < m.ny; ++y) {
-      double fl[37];
+      double fl[37] = {0};
       for (int i = 0; i < q.Q; ++i) fl[i] = f[m.idx(x, y, i)];
       const double rho = density(q, fl);
       double u[2];
@@ -1292,7 +1336,7 @@ int orc_simulate(int qid, const orc_problem* p, const orc_collision* cm, int nbc
       for (int x = 0; x < m.nx; ++x)
         for (int y = 0; y < m.ny; ++y) {
           cnt += 1;
-          double fl[37];
+          double fl[37] = {0};
           for (int i = 0; i < Q; ++i) fl[i] = f[m.idx(x, y, i)];
           const double rho = density(q, fl);
           double u[2];
@@ -1309,7 +1353,7 @@ int orc_simulate(int qid, const orc_problem* p, const orc_collision* cm, int nbc
       double err = 0.0, oldn = 0.0;
       for (int x = 0; x < m.nx; ++x)
         for (int y = 0; y < m.ny; ++y) {
-          double fl[37];
+          double fl[37] = {0};
           for (int i = 0; i < Q; ++i) fl[i] = f[m.idx(x, y, i)];
           const double rho = density(q, fl);
           double u[2];
@@ -1328,7 +1372,7 @@ int orc_simulate(int qid, const orc_problem* p, const orc_collision* cm, int nbc
       const int x = m.nx - 1, y = m.ny - 1;  // `for x_idx in nx, y_idx in ny`: one node only
       const size_t k = x + (size_t)m.nx * y;
       rho_old[k] = rho_new[k];
-      double fl[37];
+      double fl[37] = {0};
       for (int i = 0; i < Q; ++i) fl[i] = f[m.idx(x, y, i)];
       rho_new[k] = density(q, fl);
       double s = 0.0;
@@ -1412,6 +1456,60 @@ int orc_run(int qid, const orc_problem* p, const orc_collision* cm, int nbc, con
     apply_bcs(m, m.f_stream, m.f_collision);
   }
   std::memcpy(f_inout, m.f_stream.data(), n * sizeof(double));
+  return 0;
+}
+
+// Forward-mode derivative of a field loss through the time loop, for the gradient checks of
+// the adjoint: f_0 = equilibrium(1, u0) per node (maxwell_boltzmann_equilibrium.jl:12-66),
+// then `nsteps` times collide! (SRT kind 0 / TRT kind 1 with the uniform lattice force F, as
+// srt.jl:18-62 / trt.jl:42-97) and the periodic stream! (stream.jl:18-30), and
+//     L = Σ_nodes (u_x - ut_x)² + (u_y - ut_y)²,   u = velocity!(f_T) (moments.jl:1-19).
+// Every value is a Dual whose derivative part is seeded with the direction
+// (dτ_0, dτ_1, dF_x, dF_y) = seed and du0 for u0 (null: zero), so out = (L, dL/dε along it).
+// u0, ut, du0: arrays [2][ny][nx] (component, y, x).
+int orc_tangent_loss(int qid, int kind, const double* tau, const double* F, int nx, int ny, const double* u0,
+                     const double* ut, const double* seed, const double* du0, long nsteps, int nthreads,
+                     double* out) {
+  if ((kind != 0 && kind != 1) || nx <= 0 || ny <= 0 || nsteps < 0) return -1;
+  const Quad q = make_quad(qid);
+  const int Q = q.Q;
+  const size_t nn = (size_t)nx * ny, n = nn * Q;
+  auto idx = [&](int x, int y, int i) { return (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * i); };
+  const Dual t0(tau[0], seed[0]), t1(tau[1], seed[1]), Fx(F[0], seed[2]), Fy(F[1], seed[3]);
+  const bool force = F[0] != 0.0 || F[1] != 0.0 || seed[2] != 0.0 || seed[3] != 0.0;
+  std::vector<Dual> a(n), b(n);
+  for (int y = 0; y < ny; ++y)
+    for (int x = 0; x < nx; ++x) {
+      const size_t k = (size_t)y * nx + x;
+      const Dual u[2] = {Dual(u0[k], du0 ? du0[k] : 0.0), Dual(u0[nn + k], du0 ? du0[nn + k] : 0.0)};
+      Dual feq[37];
+      equilibrium(q, Dual(1.0), u, feq);
+      for (int i = 0; i < Q; ++i) a[idx(x, y, i)] = feq[i];
+    }
+  for (long t = 0; t < nsteps; ++t) {
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+    for (int x = 0; x < nx; ++x) {
+      Dual f[37], o[37];
+      for (int y = 0; y < ny; ++y) {
+        for (int i = 0; i < Q; ++i) f[i] = a[idx(x, y, i)];
+        collide_srt_trt_node<Dual>(q, kind, t0, t1, force, Fx, Fy, f, o);
+        for (int i = 0; i < Q; ++i) b[idx(x, y, i)] = o[i];
+      }
+    }
+    stream_periodic(q, nx, ny, b.data(), a.data(), nthreads);
+  }
+  Dual L = 0.0;
+  for (int y = 0; y < ny; ++y)
+    for (int x = 0; x < nx; ++x) {
+      const size_t k = (size_t)y * nx + x;
+      Dual f[37], u[2];
+      for (int i = 0; i < Q; ++i) f[i] = a[idx(x, y, i)];
+      velocity(q, (const Dual*)f, density(q, (const Dual*)f), u);
+      const Dual ex = u[0] - ut[k], ey = u[1] - ut[nn + k];
+      L += ex * ex + ey * ey;
+    }
+  out[0] = L.v;
+  out[1] = L.d;
   return 0;
 }
 

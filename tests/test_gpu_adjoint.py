@@ -92,6 +92,38 @@ def test_adjoint_matches_oracle_finite_differences(lbm_gpu, O):
     assert abs(float(np.sum(res["grad_u0"] * v)) - fd_u) <= 1e-6 * abs(fd_u)
 
 
+@pytest.mark.parametrize("kind", ["TRT", "SRT"])
+def test_adjoint_matches_oracle_forward_mode(lbm_gpu, O, kind):
+    """At 64 x 64: the adjoint's ∂L/∂τ_s, ∂L/∂τ_a, ∂L/∂F and a directional ∂L/∂u0 against the
+    forward-mode derivatives of the oracle's loop (dual numbers through its collide / stream;
+    the stand-in for ForwardDiff through the reference)."""
+    lbm = lbm_gpu
+    n, steps = 64, 200
+    u0 = lbm.divergence_free_field(n, n, kmax=8, amplitude=0.01, seed=21)
+    ut = lbm.divergence_free_field(n, n, kmax=8, amplitude=0.01, seed=22)
+    tau_s, F = 0.8, (2e-6, -1e-6)
+    tau_a = lbm.trt_magic(tau_s) if kind == "TRT" else tau_s
+    cm = lbm.TRT.fields(tau_s, tau_a) if kind == "TRT" else lbm.SRT(tau_s)
+    p = lbm.AdjointProblem(lbm.D2Q9(), n, n, cm, force=F, nsteps=steps)
+    res = p.run(u0, ut)
+    p.close()
+    v = np.random.default_rng(9).normal(size=u0.shape)
+    nt = O.max_threads()
+
+    def tangent(seed, du0=None):
+        return O.tangent_loss("D2Q9", kind, (tau_s, tau_a), F, u0, ut, steps, seed=seed, du0=du0, nthreads=nt)
+
+    L, d_ts = tangent((1, 0, 0, 0))
+    assert res["loss"] == pytest.approx(L, rel=1e-10)
+    pairs = [(res["dtau_s"], d_ts), (res["dF"][0], tangent((0, 0, 1, 0))[1]),
+             (res["dF"][1], tangent((0, 0, 0, 1))[1]),
+             (float(np.sum(res["grad_u0"] * v)), tangent((0, 0, 0, 0), v)[1])]
+    if kind == "TRT":
+        pairs.append((res["dtau_a"], tangent((0, 1, 0, 0))[1]))
+    for ad, fm in pairs:
+        assert ad == pytest.approx(fm, rel=1e-8), (ad, fm)
+
+
 def test_checkpoint_interval_does_not_change_gradients(lbm_gpu):
     lbm = lbm_gpu
     u0, ut = _fields(lbm)
