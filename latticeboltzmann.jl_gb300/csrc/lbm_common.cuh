@@ -11,6 +11,7 @@
 
 #include "../../include/lbm_gb300.h"
 #include "lbm_df64.cuh"
+#include "lbm_pf2.cuh"
 
 namespace lbm {
 
@@ -58,6 +59,29 @@ __device__ __forceinline__ dd ladd(dd a, dd b) { return add_lazy(a, b); }
 __device__ __forceinline__ dd lsub(dd a, dd b) { return add_lazy(a, -b); }
 #endif
 
+// Multiply-add shapes c + a b, c - a b, a b + c, a b - c of the collision.  FP32 / FP64: the
+// plain expressions, which the compiler contracts into FMAs; float-float: lazy sums of products;
+// packed FP32 pairs (lbm_pf2.cuh): one packed FMA.
+template <class CT>
+__device__ __forceinline__ CT add_prod(CT c, CT a, CT b) { return ladd(c, a * b); }
+template <class CT>
+__device__ __forceinline__ CT sub_prod(CT c, CT a, CT b) { return lsub(c, a * b); }
+template <class CT>
+__device__ __forceinline__ CT prod_add(CT a, CT b, CT c) { return ladd(a * b, c); }
+template <class CT>
+__device__ __forceinline__ CT prod_sub(CT a, CT b, CT c) { return lsub(a * b, c); }
+// a b + c of a value that is stored (float-float: the normalised sum)
+template <class CT>
+__device__ __forceinline__ CT prod_add_out(CT a, CT b, CT c) { return a * b + c; }
+#ifdef __CUDACC__
+// FP32: explicit FMAs, so that one node (float) and two packed nodes (pf2) round alike
+__device__ __forceinline__ float add_prod(float c, float a, float b) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float sub_prod(float c, float a, float b) { return __fmaf_rn(-a, b, c); }
+__device__ __forceinline__ float prod_add(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float prod_sub(float a, float b, float c) { return __fmaf_rn(a, b, -c); }
+__device__ __forceinline__ float prod_add_out(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+#endif
+
 // v (+)= C t for a compile-time integer C; the first term initialises v, since IEEE arithmetic
 // cannot fold a leading 0 + t away.  `set` is a constant at every point of an unrolled loop.
 template <int C, class CT>
@@ -69,7 +93,7 @@ __device__ __forceinline__ void acc_add(CT& v, bool& set, CT t) {
     v = set ? lsub(v, t) : -t;
     set = true;
   } else if constexpr (C != 0) {
-    v = set ? ladd(v, (CT)C * t) : (CT)C * t;
+    v = set ? add_prod(v, (CT)C, t) : (CT)C * t;
     set = true;
   }
 }
@@ -135,6 +159,7 @@ struct F64 {
   __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
 };
+// ld2 / st2: the values of two x-adjacent nodes as one aligned access (p at an even element).
 struct F32Dev {
   using T = float;
   using C = float;
@@ -142,6 +167,12 @@ struct F32Dev {
   static constexpr int id = LBM_STORE_F32_DEV;
   __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
+  __device__ __forceinline__ static pf2 ld2(const T* p) {
+    pf2 v;
+    v.r = __ldg(reinterpret_cast<const unsigned long long*>(p));
+    return v;
+  }
+  __device__ __forceinline__ static void st2(T* p, pf2 v) { *reinterpret_cast<unsigned long long*>(p) = v.r; }
 };
 struct F16Dev {
   using T = __half;
@@ -150,6 +181,13 @@ struct F16Dev {
   static constexpr int id = LBM_STORE_F16_DEV;
   __device__ __forceinline__ static C ld(const T* p) { return __half2float(__ldg(p)); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = __float2half_rn(v); }
+  __device__ __forceinline__ static pf2 ld2(const T* p) {
+    const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+    return pf2(f.x, f.y);
+  }
+  __device__ __forceinline__ static void st2(T* p, pf2 v) {
+    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v.lo(), v.hi());
+  }
 };
 
 struct DF64Dev {

@@ -47,6 +47,16 @@ inline void launch_step(const OpArgs& a, const StepParams<typename S::C>& p) {
   const dim3 g = lattice_grid(p.nx, p.ny);
   const auto* src = static_cast<const typename S::T*>(a.src);
   auto* dst = static_cast<typename S::T*>(a.dst);
+  if constexpr (MODE == 1 && L::Q <= 21 && (S::id == LBM_STORE_F16_DEV || S::id == LBM_STORE_F32_DEV)) {
+    // FP32 arithmetic of SRT / TRT: two nodes per thread on packed pairs (even nx).  Not for
+    // D2Q37, whose 37 pairs per thread need twice the registers of the one-node kernel (154
+    // against 72) and lose more to the lower occupancy than the packed arithmetic saves.
+    if ((a.coll == LBM_SRT || a.coll == LBM_TRT) && p.nx % 2 == 0) {
+      const dim3 g2((unsigned)((p.nx / 2 + kBlockX - 1) / kBlockX), g.y);
+      step_pair_kernel<L, S><<<g2, kBlockX, 0, a.stream>>>(p, src, dst);
+      return;
+    }
+  }
   switch (a.coll) {
     case LBM_SRT: step_kernel<L, S, LBM_SRT, MODE><<<g, kBlockX, 0, a.stream>>>(p, src, dst); break;
     case LBM_TRT: step_kernel<L, S, LBM_TRT, MODE><<<g, kBlockX, 0, a.stream>>>(p, src, dst); break;

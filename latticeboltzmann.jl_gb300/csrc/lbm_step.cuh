@@ -467,9 +467,11 @@ __host__ __device__ constexpr bool class_first(int i) {
 // polynomials in X whose coefficients depend on the node and the weight only, so they are
 // formed once per velocity class: ω_s S = b0 + X² (b2 + X² b4), ω_a A = X (ω_a w1 + a3 (c²X² - 3cJ²)).
 // FP32 keeps ω_a (w1 X) with the FP32-exact w1, so the equilibrium's momentum stays exact.
-template <class L, bool DEV, class CT>
-__device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT sFx, CT sFy, bool has_force) {
-  constexpr bool F32 = std::is_same<CT, float>::value;
+// CT is the type of the node values and PT that of the parameters: the same type, or packed FP32
+// pairs (pf2, two nodes) with FP32 parameters.
+template <class L, bool DEV, class CT, class PT>
+__device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT sFx, CT sFy, bool has_force) {
+  constexpr bool F32 = std::is_same<CT, float>::value || std::is_same<CT, pf2>::value;
   CT sp[L::Q], dp[L::Q];
   CT drho, jx, jy;
   bool sr = false, sx = false, sy = false;
@@ -495,14 +497,14 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
   const CT rho = DEV ? ladd((CT)1, drho) : drho;
   const CT inv = pair_recip(rho);
   if (has_force) {  // j' = ρ (u + τ F); a zero component adds nothing (tested on its bits, not on the FP64 pipe)
-    if (nonzero_bits(sFx)) jx = ladd(jx, rho * sFx);
-    if (nonzero_bits(sFy)) jy = ladd(jy, rho * sFy);
+    if (nonzero_bits(sFx)) jx = add_prod(jx, rho, sFx);
+    if (nonzero_bits(sFy)) jy = add_prod(jy, rho, sFy);
   }
   // node-wide, weight-free factors of b0, b2, b4 and a3
   CT D0 = drho, D2 = 0, D4 = 0, J2 = 0, c3 = 0, cs3J2 = 0, csq = 0;
   if constexpr (L::EQ >= 2) {
-    J2 = ladd(jx * jx, jy * jy);
-    D0 = lsub(drho, (p.hcs * J2) * inv);
+    J2 = prod_add(jx, jx, jy * jy);
+    D0 = sub_prod(drho, p.hcs * J2, inv);
     D2 = p.hcs2 * inv;
   }
   if constexpr (L::EQ >= 3) {
@@ -512,8 +514,8 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
   }
   if constexpr (L::EQ >= 4) {
     const CT c4 = (CT)(1.0 / 24.0) * (inv * inv) * inv;  // 1 / (24 ρ³)
-    D0 = ladd(D0, ((CT)3 * csq) * (J2 * J2) * c4);
-    D2 = lsub(D2, ((CT)6 * (csq * p.cs)) * J2 * c4);
+    D0 = add_prod(D0, ((CT)3 * csq) * (J2 * J2), c4);
+    D2 = sub_prod(D2, ((CT)6 * (csq * p.cs)) * J2, c4);
     D4 = (csq * csq) * c4;
   }
   CT b0[16], b2[16], b4[16], a3[16];
@@ -530,7 +532,7 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
   static_for<0, L::Q>([&](auto I) {
     constexpr int i = decltype(I)::value, o = L::opp(i), k = vclass<L>(i);
     if constexpr (o == i) {
-      v[i] = p.pa_s2 * v[i] + b0[k];
+      v[i] = prod_add_out(p.pa_s2, v[i], b0[k]);
     } else if constexpr (o > i) {
       CT X;
       bool xs = false;
@@ -538,19 +540,19 @@ __device__ __forceinline__ void collide_pairs(const StepParams<CT>& p, CT* v, CT
       acc_add<L::cy(i)>(X, xs, jy);
       [[maybe_unused]] const CT X2 = X * X;
       CT Se = b0[k];
-      if constexpr (L::EQ >= 4) Se = ladd(Se, X2 * ladd(b2[k], X2 * b4[k]));
-      else if constexpr (L::EQ >= 2) Se = ladd(Se, X2 * b2[k]);
+      if constexpr (L::EQ >= 4) Se = add_prod(Se, X2, add_prod(b2[k], X2, b4[k]));
+      else if constexpr (L::EQ >= 2) Se = add_prod(Se, X2, b2[k]);
       CT Ya;
       if constexpr (F32) {
         CT A = p.w1[i] * X;
-        if constexpr (L::EQ >= 3) A += (X * (csq * X2 - cs3J2)) * a3[k];
-        Ya = p.pa_a * dp[i] + p.pom_a * A;
+        if constexpr (L::EQ >= 3) A = add_prod(A, X * prod_sub(csq, X2, cs3J2), a3[k]);
+        Ya = prod_add(p.pa_a, dp[i], p.pom_a * A);
       } else {
         CT t = p.pw1a[i];
-        if constexpr (L::EQ >= 3) t = ladd(t, a3[k] * lsub(csq * X2, cs3J2));
-        Ya = ladd(p.pa_a * dp[i], t * X);
+        if constexpr (L::EQ >= 3) t = add_prod(t, a3[k], prod_sub(csq, X2, cs3J2));
+        Ya = prod_add(p.pa_a, dp[i], t * X);
       }
-      const CT Ys = ladd(p.pa_s * sp[i], Se);
+      const CT Ys = prod_add(p.pa_s, sp[i], Se);
       v[i] = Ys + Ya;
       v[o] = Ys - Ya;
     }
@@ -636,6 +638,60 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
 #pragma unroll
       for (int i = 0; i < L::Q; ++i) S::st(dst + (size_t)i * p.n + node, v[i]);
     }
+  }
+}
+
+// Fused step (MODE 1) of SRT / TRT with FP32 arithmetic, two x-adjacent nodes (x0, x0 + 1),
+// x0 even, per thread.  The collision runs on packed FP32 pairs (lbm_pf2.cuh), so its
+// arithmetic issues once for both nodes; the populations with c_x = 0 are loaded, and all
+// outputs stored, as one aligned two-node access; away from the x edges the second node's
+// addresses are the first's plus one element.  Nodes within R of an x edge, or of a y edge
+// when boundary conditions are set, are pulled by load_streamed.  Needs nx even.
+template <class L, class S>
+__global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<float> p,
+                                                            const typename S::T* __restrict__ src,
+                                                            typename S::T* __restrict__ dst) {
+  static_assert(std::is_same<typename S::C, float>::value, "packed pairs carry FP32 arithmetic");
+  using T = typename S::T;
+  const int x0 = 2 * (int)(blockIdx.x * kBlockX + threadIdx.x);
+  if (x0 >= p.nx) return;
+  const bool x_inner = x0 >= L::R && x0 + 1 + L::R < p.nx;
+  const bool has_force = p.force_kind != LBM_FORCE_NONE;
+  for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
+    const int node = y * p.nx + x0;
+    pf2 v[L::Q];
+    if (x_inner && !(p.nbc > 0 && (y < L::R || y >= p.ny - L::R))) {
+      int yo[2 * L::R + 1];
+#pragma unroll
+      for (int k = 0; k < 2 * L::R + 1; ++k) {
+        int ys = y - p.dym[k - L::R + 3];
+        ys += (ys < 0) ? p.ny : 0;
+        yo[k] = ys * p.nx;
+      }
+      static_for<0, L::Q>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        const T* a = src + (size_t)i * p.n + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
+        if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
+        else v[i] = pf2(S::ld(a), S::ld(a + 1));
+      });
+    } else {
+      float a[L::Q], b[L::Q];
+      load_streamed<L, S>(p, src, x0, y, a);
+      load_streamed<L, S>(p, src, x0 + 1, y, b);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) v[i] = pf2(a[i], b[i]);
+    }
+    pf2 sFx = 0.0f, sFy = 0.0f;
+    if (has_force) {
+      float ax, ay, bx, by;
+      node_shifted_force(p, x0, y, ax, ay);
+      node_shifted_force(p, x0 + 1, y, bx, by);
+      sFx = pf2(ax, bx);
+      sFy = pf2(ay, by);
+    }
+    collide_pairs<L, S::DEV>(p, v, sFx, sFy, has_force);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) S::st2(dst + (size_t)i * p.n + node, v[i]);
   }
 }
 
