@@ -200,6 +200,13 @@ struct DF64Dev {
     return dd(v.x, v.y);
   }
   __device__ __forceinline__ static void st(T* p, C v) { *p = make_float2(v.hi, v.lo); }
+  __device__ __forceinline__ static pdd ld2(const T* p) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    return pdd(pf2(v.x, v.z), pf2(v.y, v.w));
+  }
+  __device__ __forceinline__ static void st2(T* p, pdd v) {
+    *reinterpret_cast<float4*>(p) = make_float4(v.hi.lo(), v.lo.lo(), v.hi.hi(), v.lo.hi());
+  }
 };
 
 // ---------------------------------------------------------------------------------------

@@ -47,10 +47,12 @@ inline void launch_step(const OpArgs& a, const StepParams<typename S::C>& p) {
   const dim3 g = lattice_grid(p.nx, p.ny);
   const auto* src = static_cast<const typename S::T*>(a.src);
   auto* dst = static_cast<typename S::T*>(a.dst);
-  if constexpr (MODE == 1 && L::Q <= 21 && (S::id == LBM_STORE_F16_DEV || S::id == LBM_STORE_F32_DEV)) {
-    // FP32 arithmetic of SRT / TRT: two nodes per thread on packed pairs (even nx).  Not for
-    // D2Q37, whose 37 pairs per thread need twice the registers of the one-node kernel (154
-    // against 72) and lose more to the lower occupancy than the packed arithmetic saves.
+  // SRT / TRT of the deviation storages: two nodes per thread on packed FP32 pairs (even nx).
+  // Where the pair kernel's registers would cut the occupancy too far, the one-node kernel stays:
+  // D2Q37 in FP32 / FP16 (154 registers against 72, measured 8 % slower), and float-float above
+  // D2Q9 (D2Q13: 126 against 56).
+  constexpr bool kPairs = MODE == 1 && S::DEV && (S::id == LBM_STORE_DF64_DEV ? L::Q <= 9 : L::Q <= 25);
+  if constexpr (kPairs) {
     if ((a.coll == LBM_SRT || a.coll == LBM_TRT) && p.nx % 2 == 0) {
       const dim3 g2((unsigned)((p.nx / 2 + kBlockX - 1) / kBlockX), g.y);
       step_pair_kernel<L, S><<<g2, kBlockX, 0, a.stream>>>(p, src, dst);

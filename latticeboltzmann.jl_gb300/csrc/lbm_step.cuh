@@ -641,25 +641,26 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
   }
 }
 
-// Fused step (MODE 1) of SRT / TRT with FP32 arithmetic, two x-adjacent nodes (x0, x0 + 1),
-// x0 even, per thread.  The collision runs on packed FP32 pairs (lbm_pf2.cuh), so its
-// arithmetic issues once for both nodes; the populations with c_x = 0 are loaded, and all
-// outputs stored, as one aligned two-node access; away from the x edges the second node's
-// addresses are the first's plus one element.  Nodes within R of an x edge, or of a y edge
-// when boundary conditions are set, are pulled by load_streamed.  Needs nx even.
+// Fused step (MODE 1) of SRT / TRT with FP32 or float-float arithmetic, two x-adjacent nodes
+// (x0, x0 + 1), x0 even, per thread.  The collision runs on packed FP32 pairs (pf2 / pdd,
+// lbm_pf2.cuh), so its arithmetic issues once for both nodes; the populations with c_x = 0 are
+// loaded, and all outputs stored, as one aligned two-node access; away from the x edges the
+// second node's addresses are the first's plus one element.  Nodes within R of an x edge, or of
+// a y edge when boundary conditions are set, are pulled by load_streamed.  Needs nx even.
 template <class L, class S>
-__global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<float> p,
+__global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<typename S::C> p,
                                                             const typename S::T* __restrict__ src,
                                                             typename S::T* __restrict__ dst) {
-  static_assert(std::is_same<typename S::C, float>::value, "packed pairs carry FP32 arithmetic");
   using T = typename S::T;
+  using C = typename S::C;
+  using P = typename Packed<C>::type;
   const int x0 = 2 * (int)(blockIdx.x * kBlockX + threadIdx.x);
   if (x0 >= p.nx) return;
   const bool x_inner = x0 >= L::R && x0 + 1 + L::R < p.nx;
   const bool has_force = p.force_kind != LBM_FORCE_NONE;
   for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
     const int node = y * p.nx + x0;
-    pf2 v[L::Q];
+    P v[L::Q];
     if (x_inner && !(p.nbc > 0 && (y < L::R || y >= p.ny - L::R))) {
       int yo[2 * L::R + 1];
 #pragma unroll
@@ -672,22 +673,22 @@ __global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<float> p,
         constexpr int i = decltype(I)::value;
         const T* a = src + (size_t)i * p.n + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
         if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
-        else v[i] = pf2(S::ld(a), S::ld(a + 1));
+        else v[i] = pack2(S::ld(a), S::ld(a + 1));
       });
     } else {
-      float a[L::Q], b[L::Q];
+      C a[L::Q], b[L::Q];
       load_streamed<L, S>(p, src, x0, y, a);
       load_streamed<L, S>(p, src, x0 + 1, y, b);
 #pragma unroll
-      for (int i = 0; i < L::Q; ++i) v[i] = pf2(a[i], b[i]);
+      for (int i = 0; i < L::Q; ++i) v[i] = pack2(a[i], b[i]);
     }
-    pf2 sFx = 0.0f, sFy = 0.0f;
+    P sFx = 0, sFy = 0;
     if (has_force) {
-      float ax, ay, bx, by;
+      C ax, ay, bx, by;
       node_shifted_force(p, x0, y, ax, ay);
       node_shifted_force(p, x0 + 1, y, bx, by);
-      sFx = pf2(ax, bx);
-      sFy = pf2(ay, by);
+      sFx = pack2(ax, bx);
+      sFy = pack2(ay, by);
     }
     collide_pairs<L, S::DEV>(p, v, sFx, sFy, has_force);
 #pragma unroll
