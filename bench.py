@@ -465,7 +465,7 @@ def main():
 
     extra = {}
     if args.storage == "f64" and rank == 0 and not args.profile:
-        for st in ("df64dev", "f32dev"):
+        for st in ("df64dev", "f32dev", "f16dev"):
             _, mx, _ = build_model(lbm, st, tau_s)
             sx, _ = time_device(torch, mx, args.steps, args.warmup, dt)
             ux = mx.lattice.macroscopic()[1][:, 0]

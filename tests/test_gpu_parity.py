@@ -58,8 +58,9 @@ STORAGES = ["f64", "df64dev"]  # the FP64-class storages: both held to the 1e-12
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("qname", QUADS)
 @pytest.mark.parametrize("coll,taus", [("SRT", [0.8]), ("TRT", [0.7, 1.1]), ("MRT", [0.9, 0.75, 1.2, 0.6])])
-def test_periodic(lbm_gpu, O, qname, coll, taus, storage):
-    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, 37, 21, coll, taus, 25, storage=storage)
+@pytest.mark.parametrize("nx", [37, 36])  # odd: one node per thread; even: the two-node packed kernel
+def test_periodic(lbm_gpu, O, qname, coll, taus, storage, nx):
+    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, nx, 21, coll, taus, 25, storage=storage)
     assert rel_err(f_gpu, f_ref) <= TOL
 
 
@@ -73,23 +74,34 @@ def test_small_and_ragged_lattices(lbm_gpu, O, qname, shape, storage):
     assert rel_err(f_gpu, f_ref) <= TOL
 
 
-WALLS = [("bounce_back", "north", (1, 19), (1, 16), (0.0, 0.0)),
-         ("bounce_back", "south", (1, 19), (1, 16), (0.0, 0.0))]
-CAVITY = [("bounce_back", "east", (1, 19), (1, 16), (0.0, 0.0)),
-          ("bounce_back", "south", (1, 19), (1, 16), (0.0, 0.0)),
-          ("bounce_back", "west", (1, 19), (1, 16), (0.0, 0.0)),
-          ("moving_wall", "north", (1, 19), (1, 16), (0.004, 0.0))]
-PARTIAL = [("bounce_back", "north", (3, 11), (14, 16), (0.0, 0.0)),
-           ("bounce_back", "west", (1, 2), (5, 9), (0.0, 0.0)),
-           ("bounce_back", "south", (1, 19), (1, 1), (0.0, 0.0))]
+def _walls(nx):
+    return [("bounce_back", "north", (1, nx), (1, 16), (0.0, 0.0)),
+            ("bounce_back", "south", (1, nx), (1, 16), (0.0, 0.0))]
+
+
+def _cavity(nx):
+    return [("bounce_back", "east", (1, nx), (1, 16), (0.0, 0.0)),
+            ("bounce_back", "south", (1, nx), (1, 16), (0.0, 0.0)),
+            ("bounce_back", "west", (1, nx), (1, 16), (0.0, 0.0)),
+            ("moving_wall", "north", (1, nx), (1, 16), (0.004, 0.0))]
+
+
+def _partial(nx):
+    return [("bounce_back", "north", (3, 11), (14, 16), (0.0, 0.0)),
+            ("bounce_back", "west", (1, 2), (5, 9), (0.0, 0.0)),
+            ("bounce_back", "south", (1, nx), (1, 1), (0.0, 0.0))]
+
+
+WALLS = _walls(19)
 
 
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("qname", QUADS)
-@pytest.mark.parametrize("bcs", [WALLS, CAVITY, PARTIAL], ids=["walls", "cavity", "partial"])
+@pytest.mark.parametrize("bcs", [_walls, _cavity, _partial], ids=["walls", "cavity", "partial"])
 @pytest.mark.parametrize("coll,taus", [("SRT", [0.9]), ("TRT", [0.8, 1.05]), ("MRT", [0.8, 0.8, 0.8, 0.8])])
-def test_boundaries(lbm_gpu, O, qname, bcs, coll, taus, storage):
-    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, 19, 16, coll, taus, 20, bcs_spec=bcs, storage=storage)
+@pytest.mark.parametrize("nx", [19, 20])  # odd: one node per thread; even: the two-node packed kernel
+def test_boundaries(lbm_gpu, O, qname, bcs, coll, taus, storage, nx):
+    f_gpu, f_ref = _run_pair(lbm_gpu, O, qname, nx, 16, coll, taus, 20, bcs_spec=bcs(nx), storage=storage)
     assert rel_err(f_gpu, f_ref) <= TOL
 
 
