@@ -2,7 +2,9 @@
 // multiply-added by one packed instruction (PTX add / sub / mul / fma .rn.f32x2, sm_100 and
 // later).  Kernels that advance two nodes per thread carry every FP32 quantity of the
 // collision as a pf2 (lane 0: first node, lane 1: second node), so the arithmetic of both
-// nodes issues once.  Each lane is rounded exactly as the scalar FP32 operation.
+// nodes issues once.  Each lane is rounded exactly as the scalar FP32 operation, except that the
+// code generator may merge a product with an addition that consumes it (see pmul_exact): code
+// whose rounding must match the scalar code writes its multiply-adds as explicit FMAs.
 #pragma once
 
 #include <cuda_fp16.h>
