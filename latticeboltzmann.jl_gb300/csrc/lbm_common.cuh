@@ -82,6 +82,29 @@ __device__ __forceinline__ float prod_sub(float a, float b, float c) { return __
 __device__ __forceinline__ float prod_add_out(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 #endif
 
+// C t and v + C t for a compile-time integer C.  FP32 / FP64: a multiply and an FMA.  Float-float:
+// the product of t with an exact integer skips the FMA of the zero trailing part that a general
+// product spends, and for a power of two it is the exact scaling of both parts.
+template <int C, class CT>
+__device__ __forceinline__ CT mul_int(CT t) { return (CT)C * t; }
+template <int C, class CT>
+__device__ __forceinline__ CT add_int_prod(CT v, CT t) { return add_prod(v, (CT)C, t); }
+#ifdef __CUDACC__
+template <int C>
+__device__ __forceinline__ dd mul_int(dd t) {
+  constexpr int m = C < 0 ? -C : C;
+  constexpr float c = (float)C;
+  if constexpr ((m & (m - 1)) == 0) {
+    return dd(__fmul_rn(t.hi, c), __fmul_rn(t.lo, c));
+  } else {
+    const float p = __fmul_rn(t.hi, c);
+    return dd(p, __fmaf_rn(t.lo, c, __fmaf_rn(t.hi, c, -p)));
+  }
+}
+template <int C>
+__device__ __forceinline__ dd add_int_prod(dd v, dd t) { return add_lazy(v, mul_int<C>(t)); }
+#endif
+
 // v (+)= C t for a compile-time integer C; the first term initialises v, since IEEE arithmetic
 // cannot fold a leading 0 + t away.  `set` is a constant at every point of an unrolled loop.
 template <int C, class CT>
@@ -93,7 +116,7 @@ __device__ __forceinline__ void acc_add(CT& v, bool& set, CT t) {
     v = set ? lsub(v, t) : -t;
     set = true;
   } else if constexpr (C != 0) {
-    v = set ? add_prod(v, (CT)C, t) : (CT)C * t;
+    v = set ? add_int_prod<C>(v, t) : mul_int<C>(t);
     set = true;
   }
 }
