@@ -56,7 +56,7 @@ __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>&
   else load_streamed<L, S>(p, src, x, y, v);
   collide_node<L, S, COLL>(p, x, y, v);
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) S::st(dst + (size_t)i * p.n + node, v[i]);
+  for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
 }
 
 // One global step t over the first `nactive` members of one velocity set (members of other sets

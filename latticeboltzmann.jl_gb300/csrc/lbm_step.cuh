@@ -18,6 +18,14 @@
 
 namespace lbm {
 
+// Offset of population plane i: a 32 x 32 -> 64-bit product, since lattices have fewer than 2^31
+// nodes (lbm_create checks), so that a population's address costs two wide multiply-adds instead
+// of 64-bit multiply arithmetic.
+template <class CT>
+__device__ __forceinline__ size_t plane_off(const StepParams<CT>& p, int i) {
+  return (size_t)(unsigned)p.n * (unsigned)i;
+}
+
 // Periodic pull offsets: xw[k] = (x - (k - R)) mod nx, yo[k] = ((y - (k - R)) mod ny) * nx.
 template <class L, class CT>
 __device__ __forceinline__ void pull_offsets(const StepParams<CT>& p, int x, int y, int* xw, int* yo) {
@@ -44,7 +52,7 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) {
     const int idx = yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)];
-    f[i] = S::ld(src + (size_t)i * p.n + idx);
+    f[i] = S::ld(src + plane_off(p, i) + idx);
   }
   if (p.nbc > 0 &&
       (y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R)) {
@@ -62,13 +70,13 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
           else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
           else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
           else hit = x1 + L::cx(o) <= 0;
-          if (hit) f[i] = S::ld(src + (size_t)o * p.n + node);
+          if (hit) f[i] = S::ld(src + plane_off(p, o) + node);
         }
       } else {  // MovingWall{North}: whole top wall, ignores xs / ys
 #pragma unroll
         for (int i = 0; i < L::Q; ++i) {
           const int o = L::opp(i);
-          if (y1 + L::cy(o) > p.ny) f[i] = S::ld(src + (size_t)o * p.n + node) + (typename S::C)bc.add[i];
+          if (y1 + L::cy(o) > p.ny) f[i] = S::ld(src + plane_off(p, o) + node) + (typename S::C)bc.add[i];
         }
       }
     }
@@ -80,7 +88,7 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
 template <class L, class S, class CT>
 __device__ __forceinline__ typename S::C pop_streamed(const StepParams<CT>& p, const typename S::T* __restrict__ src,
                                                       int x, int y, const int* xw, const int* yo, bool near, int i) {
-  typename S::C v = S::ld(src + (size_t)i * p.n + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
+  typename S::C v = S::ld(src + plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
   if (near) {
     const int node = y * p.nx + x;
     const int y1 = y + 1, x1 = x + 1;
@@ -94,9 +102,9 @@ __device__ __forceinline__ typename S::C pop_streamed(const StepParams<CT>& p, c
         else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
         else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
         else hit = x1 + L::cx(o) <= 0;
-        if (hit) v = S::ld(src + (size_t)o * p.n + node);
+        if (hit) v = S::ld(src + plane_off(p, o) + node);
       } else if (y1 + L::cy(o) > p.ny) {
-        v = S::ld(src + (size_t)o * p.n + node) + (typename S::C)bc.add[i];
+        v = S::ld(src + plane_off(p, o) + node) + (typename S::C)bc.add[i];
       }
     }
   }
@@ -107,7 +115,7 @@ template <class L, class S, class CT>
 __device__ __forceinline__ void load_local(const StepParams<CT>& p, const typename S::T* __restrict__ src,
                                            int node, typename S::C* f) {
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) f[i] = S::ld(src + (size_t)i * p.n + node);
+  for (int i = 0; i < L::Q; ++i) f[i] = S::ld(src + plane_off(p, i) + node);
 }
 
 // Lattice force at node (x, y), lattice_force(problem, x, y, t) (problems.jl:103-104).
@@ -575,7 +583,7 @@ __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int
     const size_t node = (size_t)y * p.nx + x;
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
-      const CT nl = p.nonlinear[(size_t)i * p.n + node];
+      const CT nl = p.nonlinear[plane_off(p, i) + node];
       const CT feq = DEV ? p.w[i] * s + nl : p.w[i] * rho + nl;
       v[i] = p.om_a * v[i] + p.om_b * feq;
     }
@@ -611,10 +619,10 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
       CT sFx = 0, sFy = 0;
       const bool has_force = p.force_kind != LBM_FORCE_NONE;
       if (has_force) node_shifted_force(p, x, y, sFx, sFy);
-      auto out = [&](int i, CT val) { S::st(dst + (size_t)i * p.n + node, val); };
+      auto out = [&](int i, CT val) { S::st(dst + plane_off(p, i) + node, val); };
       if constexpr (MODE == 0) {
         mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
-                            [&](auto I) { return S::ld(src + (size_t)decltype(I)::value * p.n + node); }, out);
+                            [&](auto I) { return S::ld(src + plane_off(p, decltype(I)::value) + node); }, out);
       } else {
         int xw[2 * L::R + 1], yo[2 * L::R + 1];
         pull_offsets<L>(p, x, y, xw, yo);
@@ -626,7 +634,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
         } else {
           mrt_node<L, S::DEV>(p, sFx, sFy, has_force, [&](auto I) {
             constexpr int i = decltype(I)::value;
-            return S::ld(src + (size_t)i * p.n + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
+            return S::ld(src + plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
           }, out);
         }
       }
@@ -636,7 +644,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
       else load_streamed<L, S>(p, src, x, y, v);
       if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v);
 #pragma unroll
-      for (int i = 0; i < L::Q; ++i) S::st(dst + (size_t)i * p.n + node, v[i]);
+      for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
     }
   }
 }
@@ -671,7 +679,7 @@ __global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<typename 
       }
       static_for<0, L::Q>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        const T* a = src + (size_t)i * p.n + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
+        const T* a = src + plane_off(p, i) + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
         if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
         else v[i] = pack2(S::ld(a), S::ld(a + 1));
       });
@@ -692,7 +700,7 @@ __global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<typename 
     }
     collide_pairs<L, S::DEV>(p, v, sFx, sFy, has_force);
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) S::st2(dst + (size_t)i * p.n + node, v[i]);
+    for (int i = 0; i < L::Q; ++i) S::st2(dst + plane_off(p, i) + node, v[i]);
   }
 }
 
