@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
 // second node's addresses are the first's plus one element.  Nodes within R of an x edge, or of
 // a y edge when boundary conditions are set, are pulled by load_streamed.  Needs nx even.
 template <class L, class S>
-__global__ void __launch_bounds__(kBlockX) step_pair_kernel(StepParams<typename S::C> p,
+__global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <= 9) ? 10 : 0) step_pair_kernel(StepParams<typename S::C> p,
                                                             const typename S::T* __restrict__ src,
                                                             typename S::T* __restrict__ dst) {
   using T = typename S::T;
