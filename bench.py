@@ -259,6 +259,18 @@ def bench_trt_sweep(torch, lbm, every=40):
     return res
 
 
+def bench_shear_wave_study(torch, lbm):
+    """The shear-wave convergence analysis of shear_wave.ipynb for every quadrature
+    (notebook_examples.jl:34-69: DecayingShearFlow(ν, scale, static = true), its time-dependent
+    force, SRT, t_end = 1, scales 1, 2, 4, 8): 28 runs in one batch vs one simulate after another."""
+    res = lbm.run_shear_wave_study(torch=torch)
+    rows = res.pop("rows")
+    res["error_u"] = {f"{q}-{s}": r.error_u for (q, s), r in rows.items()}
+    res["workload"] = ("shear-wave convergence analysis of shear_wave.ipynb: D2Q4..D2Q37 x scales 1, 2, 4, 8, "
+                       "DecayingShearFlow(static = true) with its time-dependent force, SRT tau = 0.8, t_end = 1, FP64")
+    return res
+
+
 def bench_all_sets(torch, lbm, n=2048, steps=40):
     """Every velocity set, TRT, periodic n x n, zero-velocity start plus a constant force: the
     fused step's MLUPS and fraction of the measured HBM bandwidth per storage (2 Q sizeof(T)
@@ -482,6 +494,7 @@ def main():
     if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
         extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
                             "batched": bench_batched(torch, lbm), "trt_sweep": bench_trt_sweep(torch, lbm),
+                            "shear_wave_study": bench_shear_wave_study(torch, lbm),
                             "init": bench_init(torch, lbm), "all_sets": bench_all_sets(torch, lbm),
                             "adjoint": bench_adjoint(torch, lbm)}
     cpu = None

@@ -222,14 +222,19 @@ int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old); 
  * point in the reference, e.g. examples/notebooks/taylor_green_vortex.ipynb cell 3 and
  * examples/notebooks/trt_magic_parameter.ipynb).  A batch groups existing contexts (same
  * storage and collision model kind -- SRT, TRT or MRT --, any velocity set, FP64, float-float or
- * FP32-deviation storage, no time-dependent force) and advances member k
+ * FP32-deviation storage) and advances member k
  * by nsteps[k] steps with ONE graph launch: one kernel per global step, covering every member
  * still running.  Members keep their buffers; upload / download / reduce them as usual before
  * and after (their streams are ordered against the batch). */
 typedef struct lbm_batch lbm_batch;
 int32_t lbm_batch_create(lbm_batch** batch, lbm_ctx* const* members, int32_t count);  /* each context at most once */
 void lbm_batch_destroy(lbm_batch* batch);
-int32_t lbm_batch_step(lbm_batch* batch, const int64_t* nsteps);
+int32_t lbm_batch_step(lbm_batch* batch, const int64_t* nsteps);  /* LBM_ERR_INVALID if a member's force depends on time */
+/* The same with each member's time: step j of member k runs at physical time (t0[k] + j) dt[k],
+ * as lbm_step(member k, nsteps[k], t0[k], dt[k]) would (the loop's collide!(model, time = t * Δt),
+ * src/lattice_boltzmann_model.jl:64-67).  Needed when a member has a time-dependent force
+ * (LBM_FORCE_SHEAR, decaying_shear_flow.jl:132-147). */
+int32_t lbm_batch_step_timed(lbm_batch* batch, const int64_t* nsteps, const int64_t* t0, const double* dt);
 int32_t lbm_batch_set_stream(lbm_batch* batch, void* stream);
 int32_t lbm_batch_synchronize(lbm_batch* batch);
 int64_t lbm_batch_last_launch_count(const lbm_batch* batch);

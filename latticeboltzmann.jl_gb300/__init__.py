@@ -40,7 +40,7 @@ from .model import (LatticeBoltzmannModel, simulate, simulate_model, simulate_ba
                     apply)
 from . import build_native
 from .studies import (tgv_instances, run_tgv_study, convergence_order, trt_sweep_points, julia_range,
-                      build_trt_sweep_models, run_trt_sweep)
+                      build_trt_sweep_models, run_trt_sweep, build_shear_wave_study_models, run_shear_wave_study)
 from .adjoint import AdjointProblem, divergence_free_field, trt_magic, magic_total_derivative, LBMLoss
 
 StopCriteria = StopCriteriaFor

@@ -113,6 +113,8 @@ def lib():
         L.lbm_batch_destroy.restype = None
         L.lbm_batch_step.argtypes = [vp, C.POINTER(C.c_int64)]
         L.lbm_batch_step.restype = C.c_int32
+        L.lbm_batch_step_timed.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _DP]
+        L.lbm_batch_step_timed.restype = C.c_int32
         L.lbm_batch_set_stream.argtypes = [vp, vp]
         L.lbm_batch_set_stream.restype = C.c_int32
         L.lbm_batch_synchronize.argtypes = [vp]
@@ -146,7 +148,7 @@ EXPORTED_SYMBOLS = [
     "lbm_set_stream", "lbm_synchronize", "lbm_upload", "lbm_download", "lbm_upload_device",
     "lbm_download_device", "lbm_step", "lbm_last_launch_count", "lbm_reduce", "lbm_macroscopic",
     "lbm_collide_device", "lbm_stream_device", "lbm_apply_bcs_device", "lbm_batch_create", "lbm_batch_destroy",
-    "lbm_batch_step", "lbm_batch_set_stream", "lbm_batch_synchronize", "lbm_batch_last_launch_count",
+    "lbm_batch_step", "lbm_batch_step_timed", "lbm_batch_set_stream", "lbm_batch_synchronize", "lbm_batch_last_launch_count",
     "lbm_batch_last_error", "lbm_batch_reduce", "lbm_batch_reduce_fields", "lbm_batch_share_stream", "lbm_initialize_fields", "lbm_adjoint_create", "lbm_adjoint_destroy", "lbm_adjoint_run",
     "lbm_adjoint_last_error",
 ]

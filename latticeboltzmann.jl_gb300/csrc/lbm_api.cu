@@ -914,6 +914,7 @@ struct lbm_batch {
   int64_t graph_launches = 0;
   int64_t last_launches = 0;
   bool shared = false;             // the members issue their own work on the batch's stream
+  bool time_dependent = false;     // a member's force depends on time (its steps need their times)
   std::string err;
 };
 
@@ -982,7 +983,6 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
     if (!c || c->device != c0->device || c->storage != c0->storage || c->coll != c0->coll) return LBM_ERR_INVALID;
     if (c->coll == LBM_ITERATIVE_INIT) return LBM_ERR_UNSUPPORTED;
     if (c->storage == LBM_STORE_F16_DEV) return LBM_ERR_UNSUPPORTED;
-    if (c->force_kind == LBM_FORCE_SHEAR) return LBM_ERR_UNSUPPORTED;  // time-dependent forces
   }
   {  // a context may appear once: the batch advances each member's own buffers
     std::vector<lbm_ctx*> sorted(members, members + count);
@@ -991,6 +991,7 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
   }
   lbm_batch* b = new lbm_batch();
   b->members.assign(members, members + count);
+  for (int k = 0; k < count; ++k) b->time_dependent = b->time_dependent || members[k]->force_kind == LBM_FORCE_SHEAR;
   b->device = c0->device;
   b->storage = c0->storage;
   b->coll = c0->coll;
@@ -1088,8 +1089,13 @@ int32_t lbm_batch_synchronize(lbm_batch* b) {
 
 // Every member k advances nsteps[k] steps.  All members' steps are issued as ONE CUDA graph of
 // kernels, one per global step and velocity set, each covering every member still running.
-int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
-  if (!b || !nsteps) return LBM_ERR_INVALID;
+}  // extern "C"
+
+namespace {
+
+// One call of lbm_batch_step(_timed): t0 / dt (member order) give each member's time index at its
+// first step and its time step, or are null for members whose forces do not depend on time.
+int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, const double* dt) {
   cudaSetDevice(b->device);
   const int count = (int)b->members.size();
   for (int k = 0; k < count; ++k) {
@@ -1120,6 +1126,8 @@ int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
     d.cur0 = c->cur;
     d.phase0 = c->phase == POST_COLLIDE ? 1 : 0;
     d.pad = 0;
+    d.t0 = t0 ? (long long)t0[order[r]] : 0;
+    d.dt = dt ? dt[order[r]] : 0.0;
     end[r] = d.block_start + (c->n + kBlockX - 1) / kBlockX;
   }
   group_begin.push_back(count);
@@ -1180,6 +1188,22 @@ int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
     }
   }
   return batch_release_members(b);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t lbm_batch_step(lbm_batch* b, const int64_t* nsteps) {
+  if (!b || !nsteps) return LBM_ERR_INVALID;
+  if (b->time_dependent)
+    return bfail(b, LBM_ERR_INVALID, "a member's force depends on time: step with lbm_batch_step_timed");
+  return batch_step_impl(b, nsteps, nullptr, nullptr);
+}
+
+int32_t lbm_batch_step_timed(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, const double* dt) {
+  if (!b || !nsteps || !t0 || !dt) return LBM_ERR_INVALID;
+  return batch_step_impl(b, nsteps, t0, dt);
 }
 
 }  // extern "C"

@@ -33,6 +33,8 @@ struct BatchDyn {
   int cur0;               // buffer holding the member's state when the call starts
   int phase0;             // 0: f_stream resident (no pull, a first step collides only), 1: post-collision
   int pad;
+  long long t0;           // the member's time index at the first step of the call
+  double dt;              // its time step: step t of the call runs at physical time (t0 + t) dt
 };
 
 // Last member of the first n whose block_start <= b (block_start is ascending).
@@ -48,13 +50,13 @@ __device__ __forceinline__ int batch_find(const BatchDyn* __restrict__ dyn, int 
 
 template <class L, class S, int COLL>
 __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>& p, const typename S::T* src,
-                                                typename S::T* dst, int x, int y, bool local) {
+                                                typename S::T* dst, int x, int y, bool local, double time) {
   using CT = typename S::C;
   const int node = y * p.nx + x;
   CT v[L::Q];
   if (local) load_local<L, S>(p, src, node, v);
   else load_streamed<L, S>(p, src, x, y, v);
-  collide_node<L, S, COLL>(p, x, y, v);
+  collide_node<L, S, COLL>(p, x, y, v, time);
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
 }
@@ -81,7 +83,7 @@ __global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchStatic<t
   const T* src = static_cast<const T*>(parity ? m.buf1 : m.buf0);
   T* dst = static_cast<T*>(parity ? m.buf0 : m.buf1);
   const bool local = (t == 0) && (d.phase0 == 0);
-  batch_node_step<L, S, COLL>(p, src, dst, x, y, local);
+  batch_node_step<L, S, COLL>(p, src, dst, x, y, local, (double)(d.t0 + t) * d.dt);
 }
 
 // Reductions of many members in one launch: member d.member owns d.steps consecutive blocks

@@ -245,11 +245,20 @@ class DeviceBatch:
         if st != N.LBM_OK:
             raise N.LbmError(st, N.lib().lbm_batch_last_error(self.h).decode())
 
-    def step(self, nsteps):
+    def step(self, nsteps, t0=None, dt=None):
+        """Advance member k by nsteps[k] steps.  With t0 and dt (one per member), step j of member k
+        runs at time (t0[k] + j) dt[k], which members with a time-dependent force need."""
         ns = np.ascontiguousarray(nsteps, dtype=np.int64)
         if ns.shape != (len(self.lattices),):
             raise ValueError("one step count per member")
-        self._check(N.lib().lbm_batch_step(self.h, ns.ctypes.data_as(C.POINTER(C.c_int64))))
+        if t0 is None and dt is None:
+            self._check(N.lib().lbm_batch_step(self.h, ns.ctypes.data_as(C.POINTER(C.c_int64))))
+            return
+        t0a = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, dtype=np.int64), ns.shape))
+        dta = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), ns.shape))
+        self._check(N.lib().lbm_batch_step_timed(self.h, ns.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                  t0a.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                  dta.ctypes.data_as(N._DP)))
 
     def set_stream(self, stream_handle):
         self._check(N.lib().lbm_batch_set_stream(self.h, stream_handle or None))

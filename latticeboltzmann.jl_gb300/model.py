@@ -149,11 +149,12 @@ def simulate_batch(models, times):
     t = [b[0] for b in bounds]
     last = [b[1] for b in bounds]
     pms = [m.processing_method for m in models]
+    dts = np.array([pm.problem.delta_t() if getattr(pm, "problem", None) is not None else 0.0 for pm in pms])
     batch = DeviceBatch([m.lattice for m in models])
     batch.share_stream()
     if all(_vectorisable(pm) for pm in pms):
         try:
-            _simulate_batch_vectorised(models, pms, bounds, batch)
+            _simulate_batch_vectorised(models, pms, bounds, batch, dts)
         finally:
             batch.close()
         return models
@@ -171,8 +172,8 @@ def simulate_batch(models, times):
                 ev = pms[k].next_event(t[k] + 1)
                 nsteps[k] = last[k] - t[k] + 1 if ev is None or ev > last[k] + 1 else max(1, ev - t[k])
                 events[k] = ev
-            if nsteps.any():  # (batches hold no time-dependent force, so the steps need no time)
-                batch.step(nsteps)
+            if nsteps.any():  # step j of member k at time (t[k] + j) Δt_k, as simulate_model steps it
+                batch.step(nsteps, np.array(t, dtype=np.int64), dts)
             # members at an event (or at their final next!) and the stop reductions they will ask for
             acting = []
             for k in range(n):
@@ -217,7 +218,7 @@ def _vectorisable(pm):
                                        VelocityConvergenceStoppingCriteria))
 
 
-def _simulate_batch_vectorised(models, pms, bounds, batch):
+def _simulate_batch_vectorised(models, pms, bounds, batch, dts):
     """simulate_batch for TrackHydrodynamicErrors / CompareWithAnalyticalSolution without
     per-step processing, with the members' bookkeeping in arrays: their events (every 100 steps
     for a stop criterion, and n_steps) and their stop decisions are computed for all members at
@@ -248,7 +249,7 @@ def _simulate_batch_vectorised(models, pms, bounds, batch):
         steps = np.where(ev > last + 1, last - t + 1, np.maximum(1, ev - t))
         steps = np.where(loop, steps, 0).astype(np.int64)
         if steps.any():
-            batch.step(steps)
+            batch.step(steps, t, dts)
         t = t + steps
         act_loop = loop & (ev == t)
         act_final = stage == 1

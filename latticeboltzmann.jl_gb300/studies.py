@@ -215,3 +215,81 @@ def run_trt_sweep(points, scale=1, storage="f64", batched=True, sequential_point
             res["speedup_vs_sequential"] = res["batched_runs_per_s"] / res["sequential_runs_per_s"]
     res["rows"] = rows
     return res
+
+
+# ---------------------------------------------------------------------------------------
+# The shear-wave convergence analysis of examples/notebooks/shear_wave.ipynb
+# ---------------------------------------------------------------------------------------
+def build_shear_wave_study_models(quadratures, tau=0.8, scales=(1, 2, 4, 8), storage="f64"):
+    """The runs of shear_wave_convergence_analysis(q, AnalyticalEquilibrium(), τ; scales)
+    (examples/notebooks/notebook_examples.jl:34-69), which shear_wave.ipynb calls for every
+    quadrature: per quadrature and scale, DecayingShearFlow(ν, scale, static = true) with
+    ν = τ / (2 speed_of_sound_squared) as written there, n_steps = round(t_end / Δt) for t_end = 1,
+    TrackHydrodynamicErrors(problem, false, n_steps, NoStoppingCriteria()), the default SRT
+    collision and the analytical-equilibrium start.  The static flow carries a time-dependent
+    force (decaying_shear_flow.jl:132-147).  Returns the models, their time ranges 0:n_steps
+    and the (quadrature, scale) of each."""
+    from .collision_models import SRT
+    from .problems import DecayingShearFlow
+    from .processing_methods import NoStoppingCriteria, TrackHydrodynamicErrors
+    models, times, keys = [], [], []
+    for qname in quadratures:
+        q = Quadratures[qname]
+        nu = tau / (2.0 * q.speed_of_sound_squared)
+        for scale in scales:
+            problem = DecayingShearFlow(nu, scale, static=True)
+            n_steps = int(round(1.0 / problem.delta_t()))
+            pm = TrackHydrodynamicErrors(problem, False, n_steps, NoStoppingCriteria())
+            models.append(LatticeBoltzmannModel(problem, q, collision_model=SRT,
+                                                initialization_strategy=AnalyticalEquilibrium(), process_method=pm,
+                                                storage=storage))
+            times.append(range(0, n_steps + 1))
+            keys.append((qname, scale))
+    return models, times, keys
+
+
+def run_shear_wave_study(quadratures=("D2Q4", "D2Q5", "D2Q9", "D2Q13", "D2Q17", "D2Q21", "D2Q37"), tau=0.8,
+                         scales=(1, 2, 4, 8), storage="f64", sequential=True, torch=None):
+    """The study batched (simulate_batch: every run in one batch, the time-dependent force of each
+    member evaluated at its own step times) and, if `sequential`, once more one simulate after
+    another.  Both arms build their models first and time the time loops alone.  Returns the
+    final rows, timings, and the convergence order of error_u per quadrature."""
+    from .model import simulate_batch, simulate_model
+    if torch is None:
+        import torch
+    res = {"runs": len(quadratures) * len(scales), "storage": storage, "tau": tau, "scales": list(scales)}
+    models, times, keys = build_shear_wave_study_models(quadratures, tau, scales, storage)
+    res["lattice_updates"] = float(sum(m.lattice.nx * m.lattice.ny * (tm.stop - 1) for m, tm in zip(models, times)))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    simulate_batch(models, times)
+    torch.cuda.synchronize()
+    res["batched_s"] = time.perf_counter() - t0
+    rows = {k: m.processing_method.df[-1] for k, m in zip(keys, models)}
+    for m in models:
+        m.close()
+    if sequential:
+        models, times, _ = build_shear_wave_study_models(quadratures, tau, scales, storage)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for m, tm in zip(models, times):
+            simulate_model(m, tm)
+        torch.cuda.synchronize()
+        res["sequential_s"] = time.perf_counter() - t0
+        res["speedup_vs_sequential"] = res["sequential_s"] / res["batched_s"]
+        diffs = []
+        for k, m in zip(keys, models):
+            a, b = rows[k], m.processing_method.df[-1]
+            diffs.append(max(abs(x - y) / max(abs(y), 1e-300) for x, y in zip(a, b)
+                             if math.isfinite(x) and math.isfinite(y)))
+            m.close()
+        res["max_rel_diff_batched_vs_sequential"] = float(max(diffs))
+    orders = {}
+    for qname in quadratures:
+        xs = [math.log(8 * s) for s in scales]
+        ys = [rows[(qname, s)].error_u for s in scales]
+        if all(y > 0 and math.isfinite(y) for y in ys):
+            orders[qname] = float(-np.polyfit(xs, [math.log(y) for y in ys], 1)[0])
+    res["orders"] = orders
+    res["rows"] = rows
+    return res

@@ -2,8 +2,8 @@
 collision.  A batch runs the one-node collision on every member, so a lattice stepped alone (the
 packed kernel, for even nx) must equal the same lattice stepped in a batch bitwise — with
 bounce-back walls on every side and a moving wall (whose rows and columns take the kernel's general
-pull), with a constant and a per-node force.  The time-dependent shear force, which batches do not
-take, is checked against the FP64 run."""
+pull), with a constant, a per-node and a time-dependent force; the last is also checked against
+the FP64 run."""
 import numpy as np
 import pytest
 
@@ -12,7 +12,7 @@ from gpu_cases import wave_field
 pytestmark = pytest.mark.gpu
 
 SETS = ["D2Q4", "D2Q5", "D2Q9", "D2Q13", "D2Q17", "D2Q21"]
-CASES = ["walls_constant", "moving_wall_field", "side_walls"]
+CASES = ["walls_constant", "moving_wall_field", "side_walls", "walls_shear"]
 
 
 def _case(lbm, case, nx, ny, rng):
@@ -24,6 +24,11 @@ def _case(lbm, case, nx, ny, rng):
         ff = 1e-5 * rng.normal(size=(2, ny, nx))
         return [lbm.BounceBack(S, (1, nx), (1, ny)), lbm.MovingWall(N, (1, nx), (1, ny), (0.02, 0.0))], \
             ("field", ff)
+    if case == "walls_shear":
+        xr = (np.arange(nx) + 0.5) / nx
+        yr = (np.arange(ny) + 0.5) / ny
+        return [lbm.BounceBack(N, (1, nx), (1, ny)), lbm.BounceBack(S, (1, nx), (1, ny))], \
+            ("shear", [1e-5, 2 * np.pi, 0.01, 2e-5, 2 * np.pi, 0.02], xr, yr)
     return [lbm.BounceBack(W, (1, nx), (1, ny)), lbm.BounceBack(E, (1, nx), (1, ny))], None
 
 
@@ -41,8 +46,8 @@ def test_packed_step_equals_one_node_collision(lbm_gpu, storage, qname, case):
         solo = lbm.LatticeBoltzmannModel.from_parts(q, f0, cm, bcs, force=force, storage=storage)
         member = lbm.LatticeBoltzmannModel.from_parts(q, f0, cm, bcs, force=force, storage=storage)
         batch = lbm.DeviceBatch([member.lattice])
-        solo.lattice.step(steps, 0, 0.0)
-        batch.step([steps])
+        solo.lattice.step(steps, 3, 0.5)
+        batch.step([steps], [3], [0.5])
         fs, fb = solo.f_stream, member.f_stream
         batch.close()
         solo.close()
