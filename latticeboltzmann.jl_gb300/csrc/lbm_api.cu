@@ -915,6 +915,11 @@ struct lbm_batch {
   int64_t last_launches = 0;
   bool shared = false;             // the members issue their own work on the batch's stream
   bool time_dependent = false;     // a member's force depends on time (its steps need their times)
+  // per velocity-set group: a stream and an event, so that the groups' step chains are
+  // independent branches of the batch graph (created with the first multi-group graph)
+  std::vector<cudaStream_t> group_streams;
+  std::vector<cudaEvent_t> group_events;
+  cudaEvent_t fork = nullptr;
   std::string err;
 };
 
@@ -1042,6 +1047,9 @@ void lbm_batch_destroy(lbm_batch* b) {
   if (b->h_rout) cudaFreeHost(b->h_rout);
   if (b->done) cudaEventDestroy(b->done);
   if (b->staged) cudaEventDestroy(b->staged);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (cudaEvent_t e : b->group_events) cudaEventDestroy(e);
+  for (cudaStream_t st : b->group_streams) cudaStreamDestroy(st);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
 }
@@ -1144,22 +1152,46 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
       cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
     }
+    const int ngroups = (int)group_begin.size() - 1;
+    // the velocity-set groups advance independently: with more than one, each group's chain of
+    // steps is captured on its own stream, forked from and joined to the batch stream, so that
+    // the graph runs the chains concurrently
+    if (ngroups > 1 && (int)b->group_streams.size() < ngroups) {
+      if (!b->fork && cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bfail(b, LBM_ERR_CUDA, "event");
+      while ((int)b->group_streams.size() < ngroups) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+          return bfail(b, LBM_ERR_CUDA, "group stream");
+        b->group_streams.push_back(st);
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+          return bfail(b, LBM_ERR_CUDA, "group event");
+        b->group_events.push_back(ev);
+      }
+    }
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return bfail(b, LBM_ERR_CUDA, "begin capture");
     cudaError_t e = cudaSuccess;
-    const int ngroups = (int)group_begin.size() - 1;
-    std::vector<int> nactive(ngroups);
-    for (int gi = 0; gi < ngroups; ++gi) nactive[gi] = group_begin[gi + 1] - group_begin[gi];
+    if (ngroups > 1) {
+      e = cudaEventRecord(b->fork, b->stream);
+      for (int gi = 0; gi < ngroups && e == cudaSuccess; ++gi) e = cudaStreamWaitEvent(b->group_streams[gi], b->fork, 0);
+    }
     int64_t launches = 0;
-    for (int64_t t = 0; t < tmax && e == cudaSuccess; ++t) {
-      for (int gi = 0; gi < ngroups && e == cudaSuccess; ++gi) {
-        const int g0 = group_begin[gi];
-        while (nactive[gi] > 0 && key[g0 + nactive[gi] - 1] <= t) --nactive[gi];
-        if (nactive[gi] == 0) continue;
-        e = batch_launch(b->storage, b->coll, b->members[order[g0]]->qid, b->d_static, b->d_dyn + g0, nactive[gi],
-                         end[g0 + nactive[gi] - 1], t, b->stream);
+    for (int gi = 0; gi < ngroups && e == cudaSuccess; ++gi) {
+      const int g0 = group_begin[gi];
+      cudaStream_t st = ngroups > 1 ? b->group_streams[gi] : b->stream;
+      int nactive = group_begin[gi + 1] - g0;
+      for (int64_t t = 0; t < key[g0] && e == cudaSuccess; ++t) {  // key[g0]: the group's most steps
+        while (nactive > 0 && key[g0 + nactive - 1] <= t) --nactive;
+        e = batch_launch(b->storage, b->coll, b->members[order[g0]]->qid, b->d_static, b->d_dyn + g0, nactive,
+                         end[g0 + nactive - 1], t, st);
         ++launches;
+      }
+      if (ngroups > 1 && e == cudaSuccess) {
+        e = cudaEventRecord(b->group_events[gi], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->group_events[gi], 0);
       }
     }
     cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
