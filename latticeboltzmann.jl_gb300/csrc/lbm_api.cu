@@ -1136,7 +1136,7 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
     d.pad = 0;
     d.t0 = t0 ? (long long)t0[order[r]] : 0;
     d.dt = dt ? dt[order[r]] : 0.0;
-    end[r] = d.block_start + (c->n + kBlockX - 1) / kBlockX;
+    end[r] = d.block_start + (c->n + batch_block_nodes(b->storage) - 1) / batch_block_nodes(b->storage);
   }
   group_begin.push_back(count);
   int64_t tmax = 0;

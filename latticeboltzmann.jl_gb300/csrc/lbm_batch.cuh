@@ -61,13 +61,19 @@ __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>&
   for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
 }
 
+// Nodes per block of the batched step: 32 for FP64 storage, whose steps are bound by the FP64 pipe
+// (two instructions per SM per clock), so that a lattice of a few hundred nodes spreads over as
+// many SMs as it has warps instead of loading two or three (the 28-run shear-wave study's graph:
+// 0.071 s instead of 0.075 s); kBlockX for the other storages.
+constexpr int batch_block_nodes(int storage) { return storage == LBM_STORE_F64 ? 32 : kBlockX; }
+
 // One global step t over the first `nactive` members of one velocity set (members of other sets
-// run in their own launch of the same step).  A block covers kBlockX consecutive nodes (x
+// run in their own launch of the same step).  A block covers NB consecutive nodes (x
 // fastest) of one member: a lattice of a few nodes takes one block, so the launch keeps one
 // block per small member in flight (packing several small members into one block leaves fewer
 // warps to hide the latency of a step that is pure latency at this size; measured slower).
-template <class L, class S, int COLL>
-__global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchStatic<typename S::C>* __restrict__ statics,
+template <class L, class S, int COLL, int NB = batch_block_nodes(S::id)>
+__global__ void __launch_bounds__(NB) batch_step_kernel(const BatchStatic<typename S::C>* __restrict__ statics,
                                                              const BatchDyn* __restrict__ dyn, int nactive,
                                                              long long t) {
   using T = typename S::T;
@@ -75,7 +81,7 @@ __global__ void __launch_bounds__(kBlockX) batch_step_kernel(const BatchStatic<t
   const BatchDyn& d = dyn[batch_find(dyn, nactive, b)];
   const BatchStatic<typename S::C>& m = statics[d.member];
   const StepParams<typename S::C>& p = m.p;
-  const long long node = (b - d.block_start) * kBlockX + threadIdx.x;
+  const long long node = (b - d.block_start) * NB + threadIdx.x;
   if (node >= p.n) return;
   const int y = (int)node / p.nx;
   const int x = (int)node - y * p.nx;
@@ -134,9 +140,9 @@ cudaError_t batch_step_s(int coll, const void* statics, const BatchDyn* dyn, int
   const dim3 g((unsigned)blocks);
   const auto* m = static_cast<const BatchStatic<typename S::C>*>(statics);
   switch (coll) {
-    case LBM_SRT: batch_step_kernel<L, S, LBM_SRT><<<g, kBlockX, 0, s>>>(m, dyn, nactive, t); break;
-    case LBM_TRT: batch_step_kernel<L, S, LBM_TRT><<<g, kBlockX, 0, s>>>(m, dyn, nactive, t); break;
-    case LBM_MRT: batch_step_kernel<L, S, LBM_MRT><<<g, kBlockX, 0, s>>>(m, dyn, nactive, t); break;
+    case LBM_SRT: batch_step_kernel<L, S, LBM_SRT><<<g, batch_block_nodes(S::id), 0, s>>>(m, dyn, nactive, t); break;
+    case LBM_TRT: batch_step_kernel<L, S, LBM_TRT><<<g, batch_block_nodes(S::id), 0, s>>>(m, dyn, nactive, t); break;
+    case LBM_MRT: batch_step_kernel<L, S, LBM_MRT><<<g, batch_block_nodes(S::id), 0, s>>>(m, dyn, nactive, t); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
