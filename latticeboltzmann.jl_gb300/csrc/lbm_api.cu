@@ -104,9 +104,18 @@ struct lbm_ctx {
   double* d_analytic = nullptr;
   double* d_macro = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // time-dependent force inside graphs: {t0, bits of Δt} on the device (the graphs' steps read it
+  // and their last node advances t0), its pinned staging copy and the event of the last upload
+  long long* d_time = nullptr;
+  long long* h_time = nullptr;
+  cudaEvent_t time_ev = nullptr;
   int64_t last_launches = 0;
   std::string err;
 };
+
+// The last node of a graph of steps with a time-dependent force: the next launch starts kGraphSteps
+// steps later.
+__global__ void advance_time_kernel(long long* time, int steps) { time[0] += steps; }
 
 namespace {
 
@@ -152,6 +161,17 @@ void set_time(lbm_ctx* c, double t) {
   c->px.time = t;
 }
 
+// Steps captured into a graph read their time from the device: step k of the graph runs at
+// (t0 + k) Δt with {t0, Δt} in c->d_time (base == nullptr: back to the host-set time).
+void set_graph_time(lbm_ctx* c, const long long* base, int k) {
+  c->pd.time_base = base;
+  c->pf.time_base = base;
+  c->px.time_base = base;
+  c->pd.time_step = k;
+  c->pf.time_step = k;
+  c->px.time_step = k;
+}
+
 int ensure(lbm_ctx* c, double** p, size_t bytes) {
   if (*p) return LBM_OK;
   cudaError_t e = cudaMalloc((void**)p, bytes);
@@ -192,6 +212,12 @@ int graph_for_parity(lbm_ctx* c, int parity, cudaGraphExec_t* out) {
     *out = c->graph[parity];
     return LBM_OK;
   }
+  const bool timed = c->force_kind == LBM_FORCE_SHEAR;
+  if (timed && !c->d_time) {
+    LBM_CUDA(c, cudaMalloc((void**)&c->d_time, 2 * sizeof(long long)));
+    LBM_CUDA(c, cudaMallocHost((void**)&c->h_time, 2 * sizeof(long long)));
+    LBM_CUDA(c, cudaEventCreateWithFlags(&c->time_ev, cudaEventDisableTiming));
+  }
   const int saved_cur = c->cur, saved_phase = c->phase;
   const int64_t saved_launches = c->last_launches;
   c->cur = parity;
@@ -199,7 +225,17 @@ int graph_for_parity(lbm_ctx* c, int parity, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   LBM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = LBM_OK;
-  for (int k = 0; k < kGraphSteps && rc == LBM_OK; ++k) rc = step_once(c);
+  for (int k = 0; k < kGraphSteps && rc == LBM_OK; ++k) {
+    if (timed) set_graph_time(c, c->d_time, k);
+    rc = step_once(c);
+  }
+  if (timed) {
+    set_graph_time(c, nullptr, 0);
+    if (rc == LBM_OK) {
+      advance_time_kernel<<<1, 1, 0, c->stream>>>(c->d_time, kGraphSteps);
+      if (cudaGetLastError() != cudaSuccess) rc = fail(c, LBM_ERR_CUDA, "time advance launch");
+    }
+  }
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->cur = saved_cur;
   c->phase = saved_phase;
@@ -591,6 +627,9 @@ void lbm_destroy(lbm_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_graphs(c);
   for (int k = 0; k < 2; ++k) cudaFree(c->buf[k]);
+  cudaFree(c->d_time);
+  if (c->h_time) cudaFreeHost(c->h_time);
+  if (c->time_ev) cudaEventDestroy(c->time_ev);
   cudaFree(c->d_force);
   cudaFree(c->d_xr);
   cudaFree(c->d_yr);
@@ -725,15 +764,24 @@ int32_t lbm_step(lbm_ctx* c, int64_t nsteps, int64_t t0, double dt) {
   int64_t k = 0;
   const bool time_dependent = c->force_kind == LBM_FORCE_SHEAR;
   const size_t bytes = (size_t)c->n * c->Q * c->elem;
-  const bool use_graph = !time_dependent && bytes <= kGraphMaxBytes;
+  const bool use_graph = bytes <= kGraphMaxBytes;
+  bool time_uploaded = false;  // time-dependent force: {t0 + k, Δt} on the device for the graphs
   while (k < nsteps) {
     set_time(c, (double)(t0 + k) * dt);
     if (use_graph && c->phase == POST_COLLIDE && nsteps - k >= kGraphSteps) {
       cudaGraphExec_t g = nullptr;
       int rc = graph_for_parity(c, c->cur, &g);
       if (rc) return rc;
+      if (time_dependent && !time_uploaded) {  // the graphs that follow advance it themselves
+        LBM_CUDA(c, cudaEventSynchronize(c->time_ev));  // the staging copy is free again
+        c->h_time[0] = (long long)(t0 + k);
+        std::memcpy(&c->h_time[1], &dt, sizeof(double));
+        LBM_CUDA(c, cudaMemcpyAsync(c->d_time, c->h_time, 2 * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+        LBM_CUDA(c, cudaEventRecord(c->time_ev, c->stream));
+        time_uploaded = true;
+      }
       LBM_CUDA(c, cudaGraphLaunch(g, c->stream));
-      c->last_launches += kGraphSteps;
+      c->last_launches += kGraphSteps + (time_dependent ? 1 : 0);  // + the time advance
       k += kGraphSteps;  // even number of steps: the state returns to the same buffer
       continue;
     }

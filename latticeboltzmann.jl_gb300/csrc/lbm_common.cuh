@@ -268,6 +268,8 @@ struct StepParams {
   const double* xr;            // SHEAR coordinates (device)
   const double* yr;
   double time;                 // physical time of this step
+  const long long* time_base;  // when set: {t0, bits of Δt} on the device, and the step runs at
+  int time_step;               // time (t0 + time_step) Δt (steps of a CUDA graph, see step_time)
   const CT* nonlinear;         // ITER: nonlinear equilibrium term planes (device)
   int nbc;
   BCDev bc[LBM_MAX_BC];

@@ -118,6 +118,15 @@ __device__ __forceinline__ void load_local(const StepParams<CT>& p, const typena
   for (int i = 0; i < L::Q; ++i) f[i] = S::ld(src + plane_off(p, i) + node);
 }
 
+// Physical time of the step: p.time, or, for the steps of a captured CUDA graph of a lattice with a
+// time-dependent force, (t0 + time_step) Δt with t0 and Δt written to the device before each
+// graph launch -- the same product of the same doubles as the host's (t0 + k) Δt.
+template <class CT>
+__device__ __forceinline__ double step_time(const StepParams<CT>& p) {
+  if (!p.time_base) return p.time;
+  return (double)(p.time_base[0] + p.time_step) * __longlong_as_double(p.time_base[1]);
+}
+
 // Lattice force at node (x, y) and physical time `time`, lattice_force(problem, x, y, t)
 // (problems.jl:103-104).
 template <class CT>
@@ -574,7 +583,7 @@ __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT
 //   TRT  trt.jl:42-97    symmetric / antisymmetric parts relaxed with τ_s / τ_a, u + τ_a F
 //   MRT  mrt.jl:56-118   regularised projection (mrt_collide)
 //   ITER iterative_initialization.jl:41-60   feq = w ρ + nonlinear term
-// `time` is the physical time of the step (the step's p.time, or a batch member's own).
+// `time` is the physical time of the step (step_time(p), or a batch member's own).
 template <class L, class S, int COLL, class CT>
 __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int y, CT* v, double time) {
   constexpr bool DEV = S::DEV;
@@ -621,7 +630,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
       // rebuilt and stored one by one, so no per-node array of Q populations stays live
       CT sFx = 0, sFy = 0;
       const bool has_force = p.force_kind != LBM_FORCE_NONE;
-      if (has_force) node_shifted_force(p, x, y, sFx, sFy, p.time);
+      if (has_force) node_shifted_force(p, x, y, sFx, sFy, step_time(p));
       auto out = [&](int i, CT val) { S::st(dst + plane_off(p, i) + node, val); };
       if constexpr (MODE == 0) {
         mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
@@ -645,7 +654,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
       CT v[L::Q];
       if (MODE == 0) load_local<L, S>(p, src, node, v);
       else load_streamed<L, S>(p, src, x, y, v);
-      if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v, p.time);
+      if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v, step_time(p));
 #pragma unroll
       for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
     }
@@ -696,8 +705,9 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
     P sFx = 0, sFy = 0;
     if (has_force) {
       C ax, ay, bx, by;
-      node_shifted_force(p, x0, y, ax, ay, p.time);
-      node_shifted_force(p, x0 + 1, y, bx, by, p.time);
+      const double time = step_time(p);
+      node_shifted_force(p, x0, y, ax, ay, time);
+      node_shifted_force(p, x0 + 1, y, bx, by, time);
       sFx = pack2(ax, bx);
       sFy = pack2(ay, by);
     }

@@ -52,3 +52,26 @@ def test_shear_wave_study_batched_equals_sequential(lbm_gpu):
     res = lbm.run_shear_wave_study(("D2Q9", "D2Q17"), tau=0.8, scales=(1, 2, 4), torch=torch)
     assert res["max_rel_diff_batched_vs_sequential"] == 0.0
     assert 1.7 < res["orders"]["D2Q9"] < 2.5, res["orders"]
+
+
+@pytest.mark.parametrize("storage", ["f64", "df64dev", "f32dev"])
+@pytest.mark.parametrize("qname,nx", [("D2Q9", 24), ("D2Q17", 17)])
+def test_time_dependent_force_in_graphs_equals_single_steps(lbm_gpu, storage, qname, nx):
+    """lbm_step runs 64-step CUDA graphs also for a time-dependent force (each graph step reads
+    its time from the device): 200 steps in one call, mostly graphs, equal 20 calls of 10
+    steps, which never use a graph."""
+    lbm = lbm_gpu
+    a = _model(lbm, qname, nx, 6, storage, 1)
+    b = _model(lbm, qname, nx, 6, storage, 1)
+    t0, dt = 7, 0.013
+    a.lattice.step(200, t0, dt)
+    assert a.lattice.last_launch_count() == 200 + 3  # 3 graphs of 64 steps, each with its time advance
+    for j in range(20):
+        b.lattice.step(10, t0 + 10 * j, dt)
+    assert np.array_equal(a.f_stream, b.f_stream)
+    a.lattice.step(130, t0 + 200, dt)  # a second call: its graphs start from the new time
+    for j in range(13):
+        b.lattice.step(10, t0 + 200 + 10 * j, dt)
+    assert np.array_equal(a.f_stream, b.f_stream)
+    a.close()
+    b.close()
