@@ -48,9 +48,9 @@ __device__ __forceinline__ int batch_find(const BatchDyn* __restrict__ dyn, int 
   return lo;
 }
 
-template <class L, class S, int COLL>
+template <class L, class S, int COLL, class TimeFn>
 __device__ __forceinline__ void batch_node_step(const StepParams<typename S::C>& p, const typename S::T* src,
-                                                typename S::T* dst, int x, int y, bool local, double time) {
+                                                typename S::T* dst, int x, int y, bool local, TimeFn&& time) {
   using CT = typename S::C;
   const int node = y * p.nx + x;
   CT v[L::Q];
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(NB) batch_step_kernel(const BatchStatic<typena
   const T* src = static_cast<const T*>(parity ? m.buf1 : m.buf0);
   T* dst = static_cast<T*>(parity ? m.buf0 : m.buf1);
   const bool local = (t == 0) && (d.phase0 == 0);
-  batch_node_step<L, S, COLL>(p, src, dst, x, y, local, (double)(d.t0 + t) * d.dt);
+  batch_node_step<L, S, COLL>(p, src, dst, x, y, local, [&] { return (double)(d.t0 + t) * d.dt; });
 }
 
 // Reductions of many members in one launch: member d.member owns d.steps consecutive blocks

@@ -127,10 +127,11 @@ __device__ __forceinline__ double step_time(const StepParams<CT>& p) {
   return (double)(p.time_base[0] + p.time_step) * __longlong_as_double(p.time_base[1]);
 }
 
-// Lattice force at node (x, y) and physical time `time`, lattice_force(problem, x, y, t)
-// (problems.jl:103-104).
-template <class CT>
-__device__ __forceinline__ void node_force(const StepParams<CT>& p, int x, int y, CT& Fx, CT& Fy, double time) {
+// Lattice force at node (x, y), lattice_force(problem, x, y, t) (problems.jl:103-104).  `time()`
+// gives the physical time of the step; it is called only for the time-dependent force, so the
+// steps of the other forces spend no FP64 instruction on it.
+template <class CT, class TimeFn>
+__device__ __forceinline__ void node_force(const StepParams<CT>& p, int x, int y, CT& Fx, CT& Fy, TimeFn&& time) {
   if (p.force_kind == LBM_FORCE_CONSTANT) {
     Fx = p.F[0];
     Fy = p.F[1];
@@ -139,9 +140,9 @@ __device__ __forceinline__ void node_force(const StepParams<CT>& p, int x, int y
     Fx = (CT)__ldg(p.Ffield + k);
     Fy = (CT)__ldg(p.Ffield + p.n + k);
   } else if (p.force_kind == LBM_FORCE_SHEAR) {
-    const double X = __ldg(p.xr + x), Y = __ldg(p.yr + y);
-    Fx = (CT)(p.shear[0] * cos(p.shear[1] * Y - p.shear[2] * time));
-    Fy = (CT)(p.shear[3] * cos(p.shear[4] * X - p.shear[5] * time));
+    const double X = __ldg(p.xr + x), Y = __ldg(p.yr + y), t = time();
+    Fx = (CT)(p.shear[0] * cos(p.shear[1] * Y - p.shear[2] * t));
+    Fy = (CT)(p.shear[3] * cos(p.shear[4] * X - p.shear[5] * t));
   } else {
     Fx = 0;
     Fy = 0;
@@ -149,9 +150,9 @@ __device__ __forceinline__ void node_force(const StepParams<CT>& p, int x, int y
 }
 // Lattice force at node (x, y) times the velocity shift (τ for SRT, τ_a for TRT, τ_2 for MRT),
 // i.e. the term the collision adds to u; for a CONSTANT force the product comes from the host.
-template <class CT>
+template <class CT, class TimeFn>
 __device__ __forceinline__ void node_shifted_force(const StepParams<CT>& p, int x, int y, CT& sFx, CT& sFy,
-                                                   double time) {
+                                                   TimeFn&& time) {
   if (p.force_kind == LBM_FORCE_CONSTANT) {
     sFx = p.sF[0];
     sFy = p.sF[1];
@@ -583,9 +584,9 @@ __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT
 //   TRT  trt.jl:42-97    symmetric / antisymmetric parts relaxed with τ_s / τ_a, u + τ_a F
 //   MRT  mrt.jl:56-118   regularised projection (mrt_collide)
 //   ITER iterative_initialization.jl:41-60   feq = w ρ + nonlinear term
-// `time` is the physical time of the step (step_time(p), or a batch member's own).
-template <class L, class S, int COLL, class CT>
-__device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int y, CT* v, double time) {
+// `time()` gives the physical time of the step (step_time(p), or a batch member's own).
+template <class L, class S, int COLL, class CT, class TimeFn>
+__device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int y, CT* v, TimeFn&& time) {
   constexpr bool DEV = S::DEV;
   if constexpr (COLL == LBM_ITERATIVE_INIT) {
     CT s = v[0];
@@ -630,7 +631,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
       // rebuilt and stored one by one, so no per-node array of Q populations stays live
       CT sFx = 0, sFy = 0;
       const bool has_force = p.force_kind != LBM_FORCE_NONE;
-      if (has_force) node_shifted_force(p, x, y, sFx, sFy, step_time(p));
+      if (has_force) node_shifted_force(p, x, y, sFx, sFy, [&] { return step_time(p); });
       auto out = [&](int i, CT val) { S::st(dst + plane_off(p, i) + node, val); };
       if constexpr (MODE == 0) {
         mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
@@ -654,7 +655,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
       CT v[L::Q];
       if (MODE == 0) load_local<L, S>(p, src, node, v);
       else load_streamed<L, S>(p, src, x, y, v);
-      if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v, step_time(p));
+      if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v, [&] { return step_time(p); });
 #pragma unroll
       for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
     }
@@ -705,7 +706,7 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
     P sFx = 0, sFy = 0;
     if (has_force) {
       C ax, ay, bx, by;
-      const double time = step_time(p);
+      auto time = [&] { return step_time(p); };
       node_shifted_force(p, x0, y, ax, ay, time);
       node_shifted_force(p, x0 + 1, y, bx, by, time);
       sFx = pack2(ax, bx);
