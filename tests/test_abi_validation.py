@@ -109,6 +109,7 @@ def test_null_handles(lbm, L):
     assert L.lbm_batch_create(C.byref(h), arr, 0) == N.LBM_ERR_INVALID
     assert L.lbm_batch_create(C.byref(h), arr, 1) == N.LBM_ERR_INVALID
     assert L.lbm_batch_step(None, None) == N.LBM_ERR_INVALID
+    assert L.lbm_batch_step_timed(None, None, None, None) == N.LBM_ERR_INVALID
     assert L.lbm_batch_reduce(None, 2, None, out.ctypes.data_as(N._DP)) == N.LBM_ERR_INVALID
     assert L.lbm_batch_last_error(None).decode() == "null batch"
     L.lbm_batch_destroy(None)
