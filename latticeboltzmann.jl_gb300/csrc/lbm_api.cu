@@ -561,13 +561,9 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
     return LBM_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  // the reduction scratch (lbm_reduce) is allocated at the first reduction: members of a batch,
+  // whose reductions run batched, never need it, and a sweep creates thousands of them
   c->red_blocks = (int)std::min<int64_t>((c->n + kRedThreads - 1) / kRedThreads, 152 * 4);
-  if (cudaMalloc(&c->d_partial, (size_t)c->red_blocks * kRedMaxK * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&c->d_out, kRedMaxK * sizeof(double)) != cudaSuccess ||
-      cudaMallocHost(&c->h_out, kRedMaxK * sizeof(double)) != cudaSuccess) {
-    lbm_destroy(c);
-    return LBM_ERR_NOMEM;
-  }
   if (d->force_kind == LBM_FORCE_FIELD) {
     if (cudaMalloc(&c->d_force, (size_t)c->n * 2 * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(c->d_force, d->force_field, (size_t)c->n * 2 * sizeof(double), cudaMemcpyHostToDevice) !=
@@ -796,6 +792,10 @@ int32_t lbm_reduce(lbm_ctx* c, int32_t kind, const lbm_analytic* an, double* out
   if (!c || !out) return LBM_ERR_INVALID;
   if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
   cudaSetDevice(c->device);
+  if ((!c->d_partial && cudaMalloc(&c->d_partial, (size_t)c->red_blocks * kRedMaxK * sizeof(double)) != cudaSuccess) ||
+      (!c->d_out && cudaMalloc(&c->d_out, kRedMaxK * sizeof(double)) != cudaSuccess) ||
+      (!c->h_out && cudaMallocHost(&c->h_out, kRedMaxK * sizeof(double)) != cudaSuccess))
+    return fail(c, LBM_ERR_NOMEM, "reduction scratch");
   const bool pull = c->phase == POST_COLLIDE;
   if (kind == LBM_REDUCE_DENSITY_AT) {
     const int64_t ix = (int64_t)out[0], iy = (int64_t)out[1];

@@ -31,9 +31,11 @@ def _force_descriptor(cm, q, problem):
         return ("shear", problem.shear_force_params(), xr, yr)
     if getattr(problem, "force_is_time_dependent", False):
         raise NotImplementedError("time-dependent forces other than DecayingShearFlow's are not provided")
+    if isinstance(problem, (PoiseuilleFlow, CouetteFlow)):  # uniform: the first node's force is every node's
+        F = lattice_force_field(problem, 0.0, nodes=1)
+        return ("constant", (float(F[0].flat[0]), float(F[1].flat[0])))
     F = lattice_force_field(problem, 0.0)
-    if isinstance(problem, (PoiseuilleFlow, CouetteFlow)) or (np.all(F[0] == F[0].flat[0]) and
-                                                              np.all(F[1] == F[1].flat[0])):
+    if np.all(F[0] == F[0].flat[0]) and np.all(F[1] == F[1].flat[0]):
         return ("constant", (float(F[0].flat[0]), float(F[1].flat[0])))
     return ("field", F)
 

@@ -185,10 +185,12 @@ def node_grid(problem):
                    float(problem.domain_size[1]))[4:]
 
 
-def lattice_force_field(problem, t=0.0):
+def lattice_force_field(problem, t=0.0, nodes=None):
     """lattice_force(problem, x_idx, y_idx, t) at every node, shape (2, NY, NX)
-    (problems.jl:62-74, 103-104)."""
+    (problems.jl:62-74, 103-104); with `nodes` = 1, at node (1, 1) only, shape (2, 1, 1)."""
     X, Y = node_grid(problem)
+    if nodes == 1:
+        X, Y = X[:1, :1], Y[:1, :1]
     Fx, Fy = problem.force(X, Y, t)
     s = problem.u_max * problem.delta_t()
     out = np.empty((2,) + X.shape)
