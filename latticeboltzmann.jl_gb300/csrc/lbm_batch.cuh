@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(NB) batch_step_kernel(const BatchStatic<typena
                                                              const BatchDyn* __restrict__ dyn, int nactive,
                                                              long long t) {
   using T = typename S::T;
+  wait_prior_grid();
   const long long b = blockIdx.x;
   const BatchDyn& d = dyn[batch_find(dyn, nactive, b)];
   const BatchStatic<typename S::C>& m = statics[d.member];
@@ -140,9 +141,9 @@ cudaError_t batch_step_s(int coll, const void* statics, const BatchDyn* dyn, int
   const dim3 g((unsigned)blocks);
   const auto* m = static_cast<const BatchStatic<typename S::C>*>(statics);
   switch (coll) {
-    case LBM_SRT: batch_step_kernel<L, S, LBM_SRT><<<g, batch_block_nodes(S::id), 0, s>>>(m, dyn, nactive, t); break;
-    case LBM_TRT: batch_step_kernel<L, S, LBM_TRT><<<g, batch_block_nodes(S::id), 0, s>>>(m, dyn, nactive, t); break;
-    case LBM_MRT: batch_step_kernel<L, S, LBM_MRT><<<g, batch_block_nodes(S::id), 0, s>>>(m, dyn, nactive, t); break;
+    case LBM_SRT: launch_after_prior(batch_step_kernel<L, S, LBM_SRT>, g, batch_block_nodes(S::id), s, m, dyn, nactive, t); break;
+    case LBM_TRT: launch_after_prior(batch_step_kernel<L, S, LBM_TRT>, g, batch_block_nodes(S::id), s, m, dyn, nactive, t); break;
+    case LBM_MRT: launch_after_prior(batch_step_kernel<L, S, LBM_MRT>, g, batch_block_nodes(S::id), s, m, dyn, nactive, t); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

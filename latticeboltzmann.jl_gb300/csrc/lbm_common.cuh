@@ -82,6 +82,32 @@ __device__ __forceinline__ float prod_sub(float a, float b, float c) { return __
 __device__ __forceinline__ float prod_add_out(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 #endif
 
+#ifdef __CUDACC__
+// Programmatic dependent launch: a step kernel launched with programmatic stream serialization
+// (launch_after_prior below) may be scheduled while the previous kernel on its stream still
+// runs; it waits here, before touching global memory, until that kernel has completed and its
+// writes are visible.  For a normal launch this is a no-op.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// A step kernel launched with programmatic stream serialization: it may be scheduled while the
+// previous kernel on the stream finishes (it waits in wait_prior_grid before touching memory), so
+// the launch latency between the back-to-back steps of a graph overlaps the previous step.
+template <class... KArgs, class... Args>
+inline void launch_after_prior(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+#endif
+
 // C t and v + C t for a compile-time integer C.  FP32 / FP64: a multiply and an FMA.  Float-float:
 // the product of t with an exact integer skips the FMA of the zero trailing part that a general
 // product spends, and for a power of two it is the exact scaling of both parts.

@@ -55,15 +55,15 @@ inline void launch_step(const OpArgs& a, const StepParams<typename S::C>& p) {
   if constexpr (kPairs) {
     if ((a.coll == LBM_SRT || a.coll == LBM_TRT) && p.nx % 2 == 0) {
       const dim3 g2((unsigned)((p.nx / 2 + kBlockX - 1) / kBlockX), g.y);
-      step_pair_kernel<L, S><<<g2, kBlockX, 0, a.stream>>>(p, src, dst);
+      launch_after_prior(step_pair_kernel<L, S>, g2, kBlockX, a.stream, p, src, dst);
       return;
     }
   }
   switch (a.coll) {
-    case LBM_SRT: step_kernel<L, S, LBM_SRT, MODE><<<g, kBlockX, 0, a.stream>>>(p, src, dst); break;
-    case LBM_TRT: step_kernel<L, S, LBM_TRT, MODE><<<g, kBlockX, 0, a.stream>>>(p, src, dst); break;
-    case LBM_MRT: step_kernel<L, S, LBM_MRT, MODE><<<g, kBlockX, 0, a.stream>>>(p, src, dst); break;
-    default: step_kernel<L, S, LBM_ITERATIVE_INIT, MODE><<<g, kBlockX, 0, a.stream>>>(p, src, dst); break;
+    case LBM_SRT: launch_after_prior(step_kernel<L, S, LBM_SRT, MODE>, g, kBlockX, a.stream, p, src, dst); break;
+    case LBM_TRT: launch_after_prior(step_kernel<L, S, LBM_TRT, MODE>, g, kBlockX, a.stream, p, src, dst); break;
+    case LBM_MRT: launch_after_prior(step_kernel<L, S, LBM_MRT, MODE>, g, kBlockX, a.stream, p, src, dst); break;
+    default: launch_after_prior(step_kernel<L, S, LBM_ITERATIVE_INIT, MODE>, g, kBlockX, a.stream, p, src, dst); break;
   }
 }
 

@@ -622,6 +622,7 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C>
                                                        const typename S::T* __restrict__ src,
                                                        typename S::T* __restrict__ dst) {
   using CT = typename S::C;
+  wait_prior_grid();
   const int x = blockIdx.x * kBlockX + threadIdx.x;
   if (x >= p.nx) return;
   for (int y = blockIdx.y; y < p.ny; y += gridDim.y) {
@@ -675,6 +676,7 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
   using T = typename S::T;
   using C = typename S::C;
   using P = typename Packed<C>::type;
+  wait_prior_grid();
   const int x0 = 2 * (int)(blockIdx.x * kBlockX + threadIdx.x);
   if (x0 >= p.nx) return;
   const bool x_inner = x0 >= L::R && x0 + 1 + L::R < p.nx;
