@@ -21,13 +21,13 @@ cudaError_t adj_run(int op, int coll, const StepParams<typename S::C>& p, AdjArg
       break;
     case ADJ_STEP:
       if (coll == LBM_TRT)
-        adj_step_kernel<L, S, LBM_TRT><<<nblocks, kAdjThreads, 0, s>>>(p, a, static_cast<const T*>(src), pull,
-                                                                       static_cast<const T*>(lam_next),
-                                                                       static_cast<T*>(lam_out), slots);
+        launch_after_prior(adj_step_kernel<L, S, LBM_TRT>, dim3(nblocks), dim3(kAdjThreads), s, p, a,
+                           static_cast<const T*>(src), pull, static_cast<const T*>(lam_next),
+                           static_cast<T*>(lam_out), slots);
       else
-        adj_step_kernel<L, S, LBM_SRT><<<nblocks, kAdjThreads, 0, s>>>(p, a, static_cast<const T*>(src), pull,
-                                                                       static_cast<const T*>(lam_next),
-                                                                       static_cast<T*>(lam_out), slots);
+        launch_after_prior(adj_step_kernel<L, S, LBM_SRT>, dim3(nblocks), dim3(kAdjThreads), s, p, a,
+                           static_cast<const T*>(src), pull, static_cast<const T*>(lam_next),
+                           static_cast<T*>(lam_out), slots);
       break;
     case ADJ_U0:
       adj_u0_kernel<L, S><<<nblocks, kAdjThreads, 0, s>>>(p, u0, static_cast<const T*>(lam_next), grad);

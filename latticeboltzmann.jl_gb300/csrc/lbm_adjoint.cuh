@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(kAdjThreads, (S::DEV && L::Q <= 9) ? 4 : 1) ad
                                                                typename S::T* __restrict__ lam_out,
                                                                double* __restrict__ slots) {
   using CT = typename S::C;
+  wait_prior_grid();  // launched after the previous step's kernel (launch_after_prior)
   // per-thread sums in the compute type (a thread owns about two nodes), widened to FP64 once
   // for the block's fixed-order FP64 sum: no FP64 instruction per node
   CT tacc[kAdjParams] = {0, 0, 0, 0, 0};
