@@ -40,7 +40,8 @@ from .model import (LatticeBoltzmannModel, simulate, simulate_model, simulate_ba
                     apply)
 from . import build_native
 from .studies import (tgv_instances, run_tgv_study, convergence_order, trt_sweep_points, julia_range,
-                      build_trt_sweep_models, run_trt_sweep, build_shear_wave_study_models, run_shear_wave_study)
+                      build_trt_sweep_models, run_trt_sweep, build_shear_wave_study_models, run_shear_wave_study,
+                      SWEEP_COLUMNS, trt_sweep_table, save_sweep_table, load_sweep_table, sweep_error_grid)
 from .adjoint import AdjointProblem, divergence_free_field, trt_magic, magic_total_derivative, LBMLoss
 
 StopCriteria = StopCriteriaFor

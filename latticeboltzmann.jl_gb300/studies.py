@@ -217,6 +217,63 @@ def run_trt_sweep(points, scale=1, storage="f64", batched=True, sequential_point
     return res
 
 
+# The columns of the notebook's `results` (trt_magic_parameter.ipynb cell 2, the NamedTuple that
+# `push!(s, (τ_s = …, τ_a = …, quadrature = q, error_u = …, …))` builds, shown as a 902500×7
+# DataFrame in cell 3).
+SWEEP_COLUMNS = ("τ_s", "τ_a", "quadrature", "error_u", "error_p", "error_σ_xx", "error_σ_xy")
+
+
+def trt_sweep_table(rows, quadrature="D2Q9"):
+    """The sweep's `results` as a column table: `rows` maps (τ_s, τ_a) to the last TrackRow of
+    that run (run_trt_sweep's "rows"); the order is that of `rows` (the notebook's loop order
+    when the points came from trt_sweep_points).  Returns {column: numpy array}."""
+    keys = list(rows)
+    table = {"τ_s": np.array([k[0] for k in keys], dtype=np.float64),
+             "τ_a": np.array([k[1] for k in keys], dtype=np.float64),
+             "quadrature": np.array([quadrature] * len(keys), dtype="U8")}
+    for col in SWEEP_COLUMNS[3:]:
+        table[col] = np.array([getattr(rows[k], col) for k in keys], dtype=np.float64)
+    return table
+
+
+def save_sweep_table(path, table):
+    """Writes the table as an uncompressed .npz (one array per column, the column names as the
+    array names), the stand-in for the notebook's `@save "trt_magic_parameter_001.jld2" results`:
+    JLD2 is an HDF5 file that needs Julia or an HDF5 library, and neither is part of this
+    package's dependencies.  Julia reads the file with NPZ.jl's `npzread`."""
+    missing = [c for c in SWEEP_COLUMNS if c not in table]
+    if missing:
+        raise ValueError(f"sweep table lacks the columns {missing}")
+    n = {len(table[c]) for c in SWEEP_COLUMNS}
+    if len(n) != 1:
+        raise ValueError("sweep table columns differ in length")
+    with open(path, "wb") as fh:
+        np.savez(fh, **{c: np.asarray(table[c]) for c in SWEEP_COLUMNS})
+
+
+def load_sweep_table(path):
+    """The table save_sweep_table wrote (`@load "trt_magic_parameter_001.jld2"`, cell 5)."""
+    with np.load(path, allow_pickle=False) as z:
+        return {c: z[c].copy() for c in SWEEP_COLUMNS}
+
+
+def sweep_error_grid(table, column="error_u"):
+    """The notebook's contour input (cells 6-7): τ_ss and τ_as (the unique values in order of
+    first appearance, as `unique` gives them) and grid[a, s] = the column's value at
+    (τ_ss[s], τ_as[a]), NaN where the sweep has no such point; `contour(τ_ss, τ_as, f)`
+    evaluates f(τ_s, τ_a) over x = τ_ss, y = τ_as, so rows follow τ_a."""
+    ts = table["τ_s"]
+    ta = table["τ_a"]
+    s_vals = list(dict.fromkeys(ts.tolist()))
+    a_vals = list(dict.fromkeys(ta.tolist()))
+    s_idx = {v: k for k, v in enumerate(s_vals)}
+    a_idx = {v: k for k, v in enumerate(a_vals)}
+    grid = np.full((len(a_vals), len(s_vals)), np.nan)
+    for s, a, e in zip(ts.tolist(), ta.tolist(), np.asarray(table[column]).tolist()):
+        grid[a_idx[a], s_idx[s]] = e
+    return np.array(s_vals), np.array(a_vals), grid
+
+
 # ---------------------------------------------------------------------------------------
 # The shear-wave convergence analysis of examples/notebooks/shear_wave.ipynb
 # ---------------------------------------------------------------------------------------

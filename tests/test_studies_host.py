@@ -58,3 +58,49 @@ def test_shear_wave_study_problems(lbm, qname):
         assert c[5] != 0.0  # Fy = c3 cos(c4 x - c5 t): time enters the force
     ratios = np.array(steps[1:]) / np.array(steps[:-1])
     assert np.all(np.abs(ratios - 4.0) < 0.05), steps
+
+
+def _track_row(lbm, e):
+    vals = dict.fromkeys(lbm.processing_methods.TrackRow._fields, 0.0)
+    vals.update(timestep=100, error_u=e, error_p=2 * e, error_σ_xx=3 * e, error_σ_xy=4 * e)
+    return lbm.processing_methods.TrackRow(**vals)
+
+
+def test_sweep_table_round_trip_and_grid(lbm, tmp_path):
+    """The sweep's `results` table (trt_magic_parameter.ipynb cells 2-7): the seven columns in the
+    loop's order, written and read back unchanged, and the τ_s x τ_a grid the contour plots."""
+    taus = lbm.julia_range(0.51, 0.81, 0.1)
+    pts = lbm.trt_sweep_points(taus)
+    rows = {p: _track_row(lbm, p[0] * 10 + p[1]) for p in pts}
+    table = lbm.trt_sweep_table(rows)
+    assert tuple(table) == lbm.SWEEP_COLUMNS
+    assert len(table["τ_s"]) == 16 and table["quadrature"][0] == "D2Q9"
+    assert table["τ_s"][1] == 0.51 and table["τ_a"][1] == 0.61
+    path = tmp_path / "trt_magic_parameter_001.npz"
+    lbm.save_sweep_table(path, table)
+    back = lbm.load_sweep_table(path)
+    for c in lbm.SWEEP_COLUMNS:
+        assert np.array_equal(back[c], table[c]), c
+    ss, aa, grid = lbm.sweep_error_grid(back)
+    assert list(ss) == taus and list(aa) == taus
+    for ia, a in enumerate(aa):
+        for js, s in enumerate(ss):
+            assert grid[ia, js] == s * 10 + a
+    _, _, gp = lbm.sweep_error_grid(back, "error_p")
+    assert np.array_equal(gp, 2 * grid)
+
+
+def test_sweep_table_gaps_and_errors(lbm, tmp_path):
+    pts = [(0.6, 0.7), (0.8, 0.9)]
+    table = lbm.trt_sweep_table({p: _track_row(lbm, 1.0) for p in pts}, quadrature="D2Q17")
+    ss, aa, grid = lbm.sweep_error_grid(table)
+    assert grid[0, 0] == 1.0 and grid[1, 1] == 1.0
+    assert np.isnan(grid[0, 1]) and np.isnan(grid[1, 0])
+    bad = dict(table)
+    del bad["error_p"]
+    with pytest.raises(ValueError):
+        lbm.save_sweep_table(tmp_path / "x.npz", bad)
+    bad = dict(table)
+    bad["error_u"] = bad["error_u"][:1]
+    with pytest.raises(ValueError):
+        lbm.save_sweep_table(tmp_path / "y.npz", bad)
