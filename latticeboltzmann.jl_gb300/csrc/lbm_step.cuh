@@ -617,8 +617,11 @@ constexpr int kBlockX = 128;
 // MODE 0: collide only (first step after an upload: f_stream -> f_collision)
 // MODE 1: fused pull + boundaries + collide (post-collision -> post-collision)
 // MODE 2: pull + boundaries only (post-collision -> f_stream, materialising the observable state)
+// The float-float D2Q37 regularised MRT asks for 4 resident blocks: 128 registers without spills
+// (left alone the compiler takes 96 and spills), 6.6 against 6.2 GLUPS on the 2048^2 shear wave;
+// a bound of 6 blocks (80 registers, 84 bytes spilled) ran at 6.1.
 template <class L, class S, int COLL, int MODE>
-__global__ void __launch_bounds__(kBlockX) step_kernel(StepParams<typename S::C> p,
+__global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && S::id == LBM_STORE_DF64_DEV && L::Q == 37) ? 4 : 0) step_kernel(StepParams<typename S::C> p,
                                                        const typename S::T* __restrict__ src,
                                                        typename S::T* __restrict__ dst) {
   using CT = typename S::C;
