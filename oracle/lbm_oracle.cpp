@@ -1,6 +1,6 @@
 // lbm_oracle.cpp -- CPU restatement of LatticeBoltzmann.jl's collide-stream hot path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path: only the
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle for the CUDA path: only the
 // test-suite, the smoke check and the CPU-baseline leg of the benchmark load it.  The
 // product (liblbm_gb300.so) never links, calls or falls back to it.
 //
