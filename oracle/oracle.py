@@ -1,7 +1,7 @@
 """Python handle on the CPU oracle (``oracle/lbm_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY: the test-suite, the smoke check and the CPU-baseline leg of the
-benchmark use this module as the checker of the CUDA path.  Nothing in the product imports
+benchmark use this module as the oracle of the CUDA path.  Nothing in the product imports
 it.
 
 Arrays follow the reference's Julia layout ``f[x, y, i]`` (column-major), which is the
