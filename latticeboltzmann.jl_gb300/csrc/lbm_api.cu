@@ -119,8 +119,41 @@ __global__ void advance_time_kernel(long long* time, int steps) { time[0] += ste
 
 namespace {
 
+// A runtime call that failed (an allocation, a copy, a launch) stays the thread's last CUDA error
+// until something reads it.  Once a failure is returned as a status it is read and dropped here,
+// so that the launch check of a later, unrelated call (cudaGetLastError after its launches) does
+// not report it again.  An error that corrupts the context is not dropped by this: every later
+// call returns it.
+void drop_reported_error() { (void)cudaGetLastError(); }
+
+// Allocations that leave the pointer null when they fail, so that a destroy after a partial
+// creation frees only what was allocated.
+template <class T>
+bool dev_malloc(T** p, size_t bytes) {
+  if (cudaMalloc((void**)p, bytes) == cudaSuccess) return true;
+  *p = nullptr;
+  return false;
+}
+template <class T>
+bool host_malloc(T** p, size_t bytes) {
+  if (cudaMallocHost((void**)p, bytes) == cudaSuccess) return true;
+  *p = nullptr;
+  return false;
+}
+bool make_stream(cudaStream_t* st) {
+  if (cudaStreamCreateWithFlags(st, cudaStreamNonBlocking) == cudaSuccess) return true;
+  *st = nullptr;
+  return false;
+}
+bool make_event(cudaEvent_t* ev) {
+  if (cudaEventCreateWithFlags(ev, cudaEventDisableTiming) == cudaSuccess) return true;
+  *ev = nullptr;
+  return false;
+}
+
 int fail(lbm_ctx* c, int status, const std::string& msg) {
   if (c) c->err = msg;
+  drop_reported_error();
   return status;
 }
 
@@ -213,10 +246,11 @@ int graph_for_parity(lbm_ctx* c, int parity, cudaGraphExec_t* out) {
     return LBM_OK;
   }
   const bool timed = c->force_kind == LBM_FORCE_SHEAR;
-  if (timed && !c->d_time) {
-    LBM_CUDA(c, cudaMalloc((void**)&c->d_time, 2 * sizeof(long long)));
-    LBM_CUDA(c, cudaMallocHost((void**)&c->h_time, 2 * sizeof(long long)));
-    LBM_CUDA(c, cudaEventCreateWithFlags(&c->time_ev, cudaEventDisableTiming));
+  if (timed && !(c->d_time && c->h_time && c->time_ev)) {  // each part made once, kept if a later one fails
+    if ((!c->d_time && !dev_malloc(&c->d_time, 2 * sizeof(long long))) ||
+        (!c->h_time && !host_malloc(&c->h_time, 2 * sizeof(long long))))
+      return fail(c, LBM_ERR_NOMEM, "time slot of the step graphs");
+    if (!c->time_ev && !make_event(&c->time_ev)) return fail(c, LBM_ERR_CUDA, "time event of the step graphs");
   }
   const int saved_cur = c->cur, saved_phase = c->phase;
   const int64_t saved_launches = c->last_launches;
@@ -546,18 +580,17 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   c->red.cs = p.cs;
   c->red.q_low_order = (c->qid == LBM_D2Q4 || c->qid == LBM_D2Q5) ? 1 : 0;
 
-  cudaError_t e;
   const size_t bytes = (size_t)c->n * c->Q * c->elem;
   for (int k = 0; k < 2; ++k) {
-    e = cudaMalloc(&c->buf[k], bytes);
-    if (e != cudaSuccess) {
+    if (!dev_malloc(&c->buf[k], bytes)) {
       lbm_destroy(c);
+      drop_reported_error();
       return LBM_ERR_NOMEM;
     }
   }
-  e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) {
+  if (!make_stream(&c->own_stream)) {
     lbm_destroy(c);
+    drop_reported_error();
     return LBM_ERR_CUDA;
   }
   c->stream = c->own_stream;
@@ -565,44 +598,49 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   // whose reductions run batched, never need it, and a sweep creates thousands of them
   c->red_blocks = (int)std::min<int64_t>((c->n + kRedThreads - 1) / kRedThreads, 152 * 4);
   if (d->force_kind == LBM_FORCE_FIELD) {
-    if (cudaMalloc(&c->d_force, (size_t)c->n * 2 * sizeof(double)) != cudaSuccess ||
+    if (!dev_malloc(&c->d_force, (size_t)c->n * 2 * sizeof(double)) ||
         cudaMemcpy(c->d_force, d->force_field, (size_t)c->n * 2 * sizeof(double), cudaMemcpyHostToDevice) !=
             cudaSuccess) {
       lbm_destroy(c);
+      drop_reported_error();
       return LBM_ERR_NOMEM;
     }
   }
   if (d->force_kind == LBM_FORCE_SHEAR) {
-    if (cudaMalloc(&c->d_xr, (size_t)c->nx * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&c->d_yr, (size_t)c->ny * sizeof(double)) != cudaSuccess ||
+    if (!dev_malloc(&c->d_xr, (size_t)c->nx * sizeof(double)) ||
+        !dev_malloc(&c->d_yr, (size_t)c->ny * sizeof(double)) ||
         cudaMemcpy(c->d_xr, d->x_coords, (size_t)c->nx * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(c->d_yr, d->y_coords, (size_t)c->ny * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
       lbm_destroy(c);
+      drop_reported_error();
       return LBM_ERR_NOMEM;
     }
   }
   if (c->coll == LBM_ITERATIVE_INIT) {
     const size_t cnt = (size_t)c->n * c->Q;
     if (c->storage == LBM_STORE_F64) {
-      if (cudaMalloc(&c->d_nonlinear, cnt * sizeof(double)) != cudaSuccess ||
+      if (!dev_malloc(&c->d_nonlinear, cnt * sizeof(double)) ||
           cudaMemcpy(c->d_nonlinear, d->nonlinear, cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
         lbm_destroy(c);
+        drop_reported_error();
         return LBM_ERR_NOMEM;
       }
     } else if (c->storage == LBM_STORE_DF64_DEV) {
       std::vector<dd> tmp(cnt);
       for (size_t k = 0; k < cnt; ++k) tmp[k] = dd(d->nonlinear[k]);
-      if (cudaMalloc(&c->d_nonlinear, cnt * sizeof(dd)) != cudaSuccess ||
+      if (!dev_malloc(&c->d_nonlinear, cnt * sizeof(dd)) ||
           cudaMemcpy(c->d_nonlinear, tmp.data(), cnt * sizeof(dd), cudaMemcpyHostToDevice) != cudaSuccess) {
         lbm_destroy(c);
+        drop_reported_error();
         return LBM_ERR_NOMEM;
       }
     } else {
       std::vector<float> tmp(cnt);
       for (size_t k = 0; k < cnt; ++k) tmp[k] = (float)d->nonlinear[k];
-      if (cudaMalloc(&c->d_nonlinear, cnt * sizeof(float)) != cudaSuccess ||
+      if (!dev_malloc(&c->d_nonlinear, cnt * sizeof(float)) ||
           cudaMemcpy(c->d_nonlinear, tmp.data(), cnt * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
         lbm_destroy(c);
+        drop_reported_error();
         return LBM_ERR_NOMEM;
       }
     }
@@ -792,9 +830,9 @@ int32_t lbm_reduce(lbm_ctx* c, int32_t kind, const lbm_analytic* an, double* out
   if (!c || !out) return LBM_ERR_INVALID;
   if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
   cudaSetDevice(c->device);
-  if ((!c->d_partial && cudaMalloc(&c->d_partial, (size_t)c->red_blocks * kRedMaxK * sizeof(double)) != cudaSuccess) ||
-      (!c->d_out && cudaMalloc(&c->d_out, kRedMaxK * sizeof(double)) != cudaSuccess) ||
-      (!c->h_out && cudaMallocHost(&c->h_out, kRedMaxK * sizeof(double)) != cudaSuccess))
+  if ((!c->d_partial && !dev_malloc(&c->d_partial, (size_t)c->red_blocks * kRedMaxK * sizeof(double))) ||
+      (!c->d_out && !dev_malloc(&c->d_out, kRedMaxK * sizeof(double))) ||
+      (!c->h_out && !host_malloc(&c->h_out, kRedMaxK * sizeof(double))))
     return fail(c, LBM_ERR_NOMEM, "reduction scratch");
   const bool pull = c->phase == POST_COLLIDE;
   if (kind == LBM_REDUCE_DENSITY_AT) {
@@ -975,6 +1013,7 @@ namespace {
 
 int bfail(lbm_batch* b, int status, const std::string& msg) {
   if (b) b->err = msg;
+  drop_reported_error();
   return status;
 }
 
@@ -1058,16 +1097,15 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
     else if (b->storage == LBM_STORE_DF64_DEV) fill_static(*reinterpret_cast<BatchStatic<dd>*>(slot), c->px, c);
     else fill_static(*reinterpret_cast<BatchStatic<float>*>(slot), c->pf, c);
   }
-  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming) != cudaSuccess ||
-      cudaMalloc(&b->d_static, sb * count) != cudaSuccess ||
-      cudaMalloc((void**)&b->d_dyn, sizeof(BatchDyn) * count) != cudaSuccess ||
-      cudaMallocHost((void**)&b->h_dyn, sizeof(BatchDyn) * count) != cudaSuccess ||
-      cudaMalloc((void**)&b->d_rout, sizeof(double) * kRedMaxK * count) != cudaSuccess ||
-      cudaMallocHost((void**)&b->h_rout, sizeof(double) * kRedMaxK * count) != cudaSuccess ||
+  if (!make_stream(&b->own_stream) || !make_event(&b->done) || !make_event(&b->staged) ||
+      !dev_malloc(&b->d_static, sb * count) ||
+      !dev_malloc((void**)&b->d_dyn, sizeof(BatchDyn) * count) ||
+      !host_malloc((void**)&b->h_dyn, sizeof(BatchDyn) * count) ||
+      !dev_malloc((void**)&b->d_rout, sizeof(double) * kRedMaxK * count) ||
+      !host_malloc((void**)&b->h_rout, sizeof(double) * kRedMaxK * count) ||
       cudaMemcpy(b->d_static, h.data(), sb * count, cudaMemcpyHostToDevice) != cudaSuccess) {
     lbm_batch_destroy(b);
+    drop_reported_error();
     return LBM_ERR_NOMEM;
   }
   b->stream = b->own_stream;
@@ -1204,17 +1242,16 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
     // the velocity-set groups advance independently: with more than one, each group's chain of
     // steps is captured on its own stream, forked from and joined to the batch stream, so that
     // the graph runs the chains concurrently
-    if (ngroups > 1 && (int)b->group_streams.size() < ngroups) {
-      if (!b->fork && cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
-        return bfail(b, LBM_ERR_CUDA, "event");
+    if (ngroups > 1) {  // streams and events are kept when a later one fails, so each is counted on its own
+      if (!b->fork && !make_event(&b->fork)) return bfail(b, LBM_ERR_CUDA, "event");
       while ((int)b->group_streams.size() < ngroups) {
         cudaStream_t st = nullptr;
-        cudaEvent_t ev = nullptr;
-        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
-          return bfail(b, LBM_ERR_CUDA, "group stream");
+        if (!make_stream(&st)) return bfail(b, LBM_ERR_CUDA, "group stream");
         b->group_streams.push_back(st);
-        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
-          return bfail(b, LBM_ERR_CUDA, "group event");
+      }
+      while ((int)b->group_events.size() < ngroups) {
+        cudaEvent_t ev = nullptr;
+        if (!make_event(&ev)) return bfail(b, LBM_ERR_CUDA, "group event");
         b->group_events.push_back(ev);
       }
     }
@@ -1305,7 +1342,7 @@ int batch_ensure_rargs(lbm_batch* b) {
     b->h_rargs[k] = c->red;
     b->h_rargs[k].u_old = c->d_uold;
   }
-  if (cudaMalloc((void**)&b->d_rargs, sizeof(ReduceArgs) * count) != cudaSuccess)
+  if (!dev_malloc((void**)&b->d_rargs, sizeof(ReduceArgs) * count))
     return bfail(b, LBM_ERR_NOMEM, "reduction arguments");
   if (cudaMemcpy(b->d_rargs, b->h_rargs.data(), sizeof(ReduceArgs) * count, cudaMemcpyHostToDevice) != cudaSuccess)
     return bfail(b, LBM_ERR_CUDA, "reduction arguments");
@@ -1348,7 +1385,7 @@ int batch_reduce_run(lbm_batch* b, int K, const std::vector<int>& selected, cons
   if (total > b->rpartial_blocks) {
     cudaFree(b->d_rpartial);
     b->d_rpartial = nullptr;
-    if (cudaMalloc((void**)&b->d_rpartial, sizeof(double) * kRedMaxK * total) != cudaSuccess) {
+    if (!dev_malloc((void**)&b->d_rpartial, sizeof(double) * kRedMaxK * total)) {
       b->rpartial_blocks = 0;
       return bfail(b, LBM_ERR_NOMEM, "reduction partials");
     }
@@ -1435,12 +1472,12 @@ int32_t lbm_batch_reduce_fields(lbm_batch* b, int32_t kind, const uint8_t* selec
     b->d_ranal = nullptr;
     b->h_ranal = nullptr;
     b->ranal_cap = 0;
-    if (cudaMalloc((void**)&b->d_ranal, total * sizeof(double)) != cudaSuccess ||
-        cudaMallocHost((void**)&b->h_ranal, total * sizeof(double)) != cudaSuccess)
+    if (!dev_malloc((void**)&b->d_ranal, total * sizeof(double)) ||
+        !host_malloc((void**)&b->h_ranal, total * sizeof(double)))
       return bfail(b, LBM_ERR_NOMEM, "analytic staging");
     b->ranal_cap = total;
   }
-  if (!b->d_rargs_call && cudaMalloc((void**)&b->d_rargs_call, sizeof(ReduceArgs) * count) != cudaSuccess)
+  if (!b->d_rargs_call && !dev_malloc((void**)&b->d_rargs_call, sizeof(ReduceArgs) * count))
     return bfail(b, LBM_ERR_NOMEM, "reduction arguments");
   // pack the planes (the pinned staging is free: the previous call ended with a synchronize)
   std::vector<ReduceArgs> args = b->h_rargs;
@@ -1509,6 +1546,7 @@ namespace {
 
 int afail(lbm_adjoint* a, int status, const std::string& msg) {
   if (a) a->err = msg;
+  drop_reported_error();
   return status;
 }
 
@@ -1612,19 +1650,19 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
   a->nck = (a->T + a->k - 1) / a->k;
   a->bytes = (size_t)c->n * c->Q * c->elem;
   a->nblocks = (int)std::min<int64_t>((c->n + kAdjThreads - 1) / kAdjThreads, 152 * 4);
-  bool ok = cudaMalloc(&a->a0, a->bytes) == cudaSuccess && cudaMalloc(&a->fwd[0], a->bytes) == cudaSuccess &&
-            cudaMalloc(&a->fwd[1], a->bytes) == cudaSuccess && cudaMalloc(&a->lam[0], a->bytes) == cudaSuccess &&
-            cudaMalloc(&a->lam[1], a->bytes) == cudaSuccess &&
-            cudaMalloc(&a->d_u0, (size_t)c->n * 2 * sizeof(double)) == cudaSuccess &&
-            cudaMalloc(&a->d_ut, (size_t)c->n * 2 * sizeof(double)) == cudaSuccess &&
-            cudaMalloc(&a->d_grad, (size_t)c->n * 2 * sizeof(double)) == cudaSuccess &&
-            cudaMalloc(&a->d_slots, (size_t)a->nblocks * (1 + kAdjParams) * sizeof(double)) == cudaSuccess &&
-            cudaMalloc(&a->d_out, 8 * sizeof(double)) == cudaSuccess &&
-            cudaMallocHost(&a->h_out, 8 * sizeof(double)) == cudaSuccess;
+  bool ok = dev_malloc(&a->a0, a->bytes) && dev_malloc(&a->fwd[0], a->bytes) &&
+            dev_malloc(&a->fwd[1], a->bytes) && dev_malloc(&a->lam[0], a->bytes) &&
+            dev_malloc(&a->lam[1], a->bytes) &&
+            dev_malloc(&a->d_u0, (size_t)c->n * 2 * sizeof(double)) &&
+            dev_malloc(&a->d_ut, (size_t)c->n * 2 * sizeof(double)) &&
+            dev_malloc(&a->d_grad, (size_t)c->n * 2 * sizeof(double)) &&
+            dev_malloc(&a->d_slots, (size_t)a->nblocks * (1 + kAdjParams) * sizeof(double)) &&
+            dev_malloc(&a->d_out, 8 * sizeof(double)) &&
+            host_malloc(&a->h_out, 8 * sizeof(double));
   a->ckpt.assign(a->nck, nullptr);
-  for (int64_t cc = 1; ok && cc < a->nck; ++cc) ok = cudaMalloc(&a->ckpt[cc], a->bytes) == cudaSuccess;
+  for (int64_t cc = 1; ok && cc < a->nck; ++cc) ok = dev_malloc(&a->ckpt[cc], a->bytes);
   a->seg.assign(a->k, nullptr);
-  for (int64_t j = 0; ok && j < a->k; ++j) ok = cudaMalloc(&a->seg[j], a->bytes) == cudaSuccess;
+  for (int64_t j = 0; ok && j < a->k; ++j) ok = dev_malloc(&a->seg[j], a->bytes);
   if (!ok) {
     lbm_adjoint_destroy(a);
     return fail(c, LBM_ERR_NOMEM, "adjoint: device memory for checkpoints");

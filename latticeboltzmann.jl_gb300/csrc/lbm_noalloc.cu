@@ -83,7 +83,10 @@ extern "C" int32_t lbm_reduce_noalloc(int32_t quadrature, const double* weights,
   if ((int64_t)nblocks * K > kNoAllocSlots) return LBM_ERR_INVALID;
 
   double* scratch = nullptr;
-  if (scratch_address(&scratch) != cudaSuccess) return LBM_ERR_CUDA;
+  if (scratch_address(&scratch) != cudaSuccess) {
+    (void)cudaGetLastError();  // reported as the status: not left for a later launch check to find
+    return LBM_ERR_CUDA;
+  }
 
   // Kernel parameters on the stack: only the fields the reductions read are set.
   StepParams<double> p{};

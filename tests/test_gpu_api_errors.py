@@ -39,6 +39,22 @@ def test_state_and_argument_errors(lbm_gpu):
     lat.close()
 
 
+def test_failed_allocation_is_not_reported_again(lbm_gpu):
+    """A lattice too large for the device (D2Q37 FP64, 46000 x 46000 nodes: 626 GB per population
+    array, under the 2^31-node limit) is refused with LBM_ERR_NOMEM at its first allocation; the
+    failed allocation stays out of the launch checks of later, unrelated calls."""
+    lbm = lbm_gpu
+    N = lbm._native
+    with pytest.raises(N.LbmError) as e:
+        _lattice(lbm, "D2Q37", "f64", lbm.SRT(0.8), nx=46000, ny=46000)
+    assert e.value.status == N.LBM_ERR_NOMEM
+    lat = _lattice(lbm)
+    lat.initialize_fields()
+    lat.step(5)
+    assert abs(lat.conserved()[0] - 12 * 10) < 1e-12
+    lat.close()
+
+
 def test_non_finite_populations_are_reported(lbm_gpu):
     lbm = lbm_gpu
     N = lbm._native
