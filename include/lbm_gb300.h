@@ -225,7 +225,8 @@ int32_t lbm_apply_bcs_device(lbm_ctx* ctx, double* f_new, const double* f_old); 
  * FP32-deviation storage) and advances member k
  * by nsteps[k] steps with ONE graph launch: one kernel per global step, covering every member
  * still running.  Members keep their buffers; upload / download / reduce them as usual before
- * and after (their streams are ordered against the batch). */
+ * and after (their streams are ordered against the batch).  The batch holds its members'
+ * contexts without owning them: destroy the batch before any of its members. */
 typedef struct lbm_batch lbm_batch;
 int32_t lbm_batch_create(lbm_batch** batch, lbm_ctx* const* members, int32_t count);  /* each context at most once */
 void lbm_batch_destroy(lbm_batch* batch);

@@ -7,6 +7,7 @@ a C-contiguous float64 array of shape (Q, NY, NX).
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -112,6 +113,10 @@ class DeviceLattice:
 
     # ---- lifetime ----------------------------------------------------------------------
     def close(self):
+        # a batch holds this context without owning it (and may have lent it its stream), so any
+        # open batch of this lattice goes first
+        for b in list(getattr(self, "_batches", ())):
+            b.close()
         if getattr(self, "h", None):
             N.lib().lbm_destroy(self.h)
             self.h = None
@@ -227,19 +232,35 @@ class DeviceLattice:
 class DeviceBatch:
     """Several DeviceLattices advanced together: member k takes nsteps[k] steps, all issued as one
     CUDA graph with one kernel per global step over every member still running (lbm_batch_*).
-    Members must share storage (f64, df64dev or f32dev) and collision kind (SRT, TRT or MRT) and have no
-    time-dependent force."""
+    Members must share storage (f64, df64dev or f32dev) and collision kind (SRT, TRT or MRT); members
+    with a time-dependent force are stepped with their times (step(nsteps, t0, dt)).  The batch holds
+    its members' contexts without owning them: close the batch before any member."""
 
     def __init__(self, lattices):
         L = N.lib()
         self.lattices = list(lattices)
+        if any(not getattr(lat, "h", None) for lat in self.lattices):
+            raise ValueError("a batch member is closed")
         arr = (C.c_void_p * len(self.lattices))(*[lat.h.value for lat in self.lattices])
         h = C.c_void_p()
         st = L.lbm_batch_create(C.byref(h), arr, len(self.lattices))
         if st != N.LBM_OK:
             raise N.LbmError(st, "lbm_batch_create: members must share storage and collision kind (SRT, TRT, MRT), "
-                                 "use f64 / df64dev / f32dev and no time-dependent force")
+                                 "use f64 / df64dev / f32dev, and each appear once")
         self.h = h
+        for lat in self.lattices:  # weak: the batch's references keep the members, not the other way
+            if not hasattr(lat, "_batches"):
+                lat._batches = weakref.WeakSet()
+            lat._batches.add(self)
+
+    def _open(self):
+        """The batch and every member still open: the library holds the members' contexts, so a
+        member closed first would leave it a freed context."""
+        if not getattr(self, "h", None):
+            raise ValueError("the batch is closed")
+        for k, lat in enumerate(self.lattices):
+            if not getattr(lat, "h", None):
+                raise ValueError(f"batch member {k} was closed before its batch")
 
     def _check(self, st):
         if st != N.LBM_OK:
@@ -248,6 +269,7 @@ class DeviceBatch:
     def step(self, nsteps, t0=None, dt=None):
         """Advance member k by nsteps[k] steps.  With t0 and dt (one per member), step j of member k
         runs at time (t0[k] + j) dt[k], which members with a time-dependent force need."""
+        self._open()
         ns = np.ascontiguousarray(nsteps, dtype=np.int64)
         if ns.shape != (len(self.lattices),):
             raise ValueError("one step count per member")
@@ -261,9 +283,11 @@ class DeviceBatch:
                                                   dta.ctypes.data_as(N._DP)))
 
     def set_stream(self, stream_handle):
+        self._open()
         self._check(N.lib().lbm_batch_set_stream(self.h, stream_handle or None))
 
     def synchronize(self):
+        self._open()
         self._check(N.lib().lbm_batch_synchronize(self.h))
 
     def last_launch_count(self) -> int:
@@ -272,6 +296,7 @@ class DeviceBatch:
     def reduce(self, kind, select=None):
         """lbm_batch_reduce: the (members, K) sums of a stop-criterion reduction of the selected
         members (all when select is None; rows of unselected members are zero)."""
+        self._open()
         out = np.zeros((len(self.lattices), 16))
         sel = None
         if select is not None:
@@ -287,6 +312,7 @@ class DeviceBatch:
         """lbm_batch_reduce_fields: the TRACK_ERRORS / COMPARE sums of the members for which
         `inputs[k]` = (fields dict of (NY, NX) host planes, tau, u_max, area) is given (None:
         not selected); rows of unselected members are zero."""
+        self._open()
         n = len(self.lattices)
         sel = np.zeros(n, dtype=np.uint8)
         an = (N.LbmAnalytic * n)()
@@ -311,6 +337,7 @@ class DeviceBatch:
 
     def share_stream(self):
         """lbm_batch_share_stream: members issue their own work on the batch's stream."""
+        self._open()
         self._check(N.lib().lbm_batch_share_stream(self.h))
 
     def close(self):
