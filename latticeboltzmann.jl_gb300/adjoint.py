@@ -37,9 +37,13 @@ class AdjointProblem:
 
     def run(self, u0, u_target, want_grad_u0=True):
         """u0, u_target: arrays of shape (2, NY, NX).  Returns a dict with the loss and gradients."""
+        if not getattr(self, "h", None):
+            raise ValueError("the adjoint problem is closed")
         u0 = np.ascontiguousarray(u0, dtype=np.float64)
         ut = np.ascontiguousarray(u_target, dtype=np.float64)
-        assert u0.shape == (2, self.ny, self.nx) and ut.shape == u0.shape
+        if u0.shape != (2, self.ny, self.nx) or ut.shape != u0.shape:
+            raise ValueError(f"u0 and u_target must have shape (2, {self.ny}, {self.nx}), "
+                             f"got {u0.shape} and {ut.shape}")
         res = np.zeros(8)
         g = np.zeros_like(u0) if want_grad_u0 else None
         st = N.lib().lbm_adjoint_run(self.h, u0.ctypes.data_as(N._DP), ut.ctypes.data_as(N._DP),

@@ -4,6 +4,7 @@ closes every open batch that holds it."""
 import ctypes as C
 import weakref
 
+import numpy as np
 import pytest
 
 
@@ -47,3 +48,21 @@ def test_closing_a_member_closes_its_batches_first(lbm):
 def test_batch_of_a_closed_lattice_is_refused(lbm):
     with pytest.raises(ValueError, match="member is closed"):
         lbm.device.DeviceBatch([_Closed()])
+
+
+def test_adjoint_run_checks_its_inputs_before_the_library(lbm):
+    AdjointProblem = lbm.adjoint.AdjointProblem
+    a = object.__new__(AdjointProblem)
+    a.h, a.nx, a.ny = None, 8, 6
+    a.lattice = _Closed()
+    a.lattice.close = lambda: None
+    with pytest.raises(ValueError, match="closed"):
+        a.run(np.zeros((2, 6, 8)), np.zeros((2, 6, 8)))
+    a.h = C.c_void_p(1)  # never passed to the library: the shapes are checked first
+    try:
+        with pytest.raises(ValueError, match="shape"):
+            a.run(np.zeros((2, 8, 6)), np.zeros((2, 8, 6)))
+        with pytest.raises(ValueError, match="shape"):
+            a.run(np.zeros((2, 6, 8)), np.zeros((2, 6, 7)))
+    finally:
+        a.h = None
