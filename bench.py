@@ -164,28 +164,56 @@ def time_e2e(torch, lbm, problem, model, f0, steps, dt):
     return start.elapsed_time(end) / 1e3, host_in.numel() * 8, host_out.numel() * 8
 
 
-def cpu_baseline(tau_s, budget_s=12.0):
-    """The oracle port (collide -> stream -> bounce-back, OpenMP over x) on the host cores, on
-    a bounded sample of the workload: whole 4096^2 time steps, as many as fit the budget."""
-    from oracle import oracle as O
-    threads = O.max_threads()
+def oracle_channel(O, tau_s, nx=NX, ny=NY):
+    """The benchmark channel as oracle inputs: problem, TRT collision with the force, the
+    bounce-back walls and the zero-velocity start (f = w)."""
     nu = (tau_s - 0.5) / 3.0
-    p = O.poiseuille_struct(1.0, 0.05, nu, NX, NY, 1.0, (1.0, 1.0), 1.0)
+    p = O.poiseuille_struct(1.0, 0.05, nu, nx, ny, 1.0, (1.0, 1.0), 1.0)
     sc = O.problem_scalars(p)
     p.G = 1e-6 / (0.05 * sc["delta_t"] * sc["viscosity"])
     cm = O.collision("TRT", [tau_s, 0.5 + 0.25 / (tau_s - 0.5)], force=True)
-    bcs = [O.bc("bounce_back", "north", (1, NX), (1, NY)), O.bc("bounce_back", "south", (1, NX), (1, NY))]
-    f = O.initialize(O.INIT_ZERO_VELOCITY, "D2Q9", p)
+    bcs = [O.bc("bounce_back", "north", (1, nx), (1, ny)), O.bc("bounce_back", "south", (1, nx), (1, ny))]
+    return p, cm, bcs, O.initialize(O.INIT_ZERO_VELOCITY, "D2Q9", p), sc["delta_t"]
+
+
+def cpu_rate(tau_s, threads, budget_s):
+    """The oracle port (collide -> stream -> bounce-back, OpenMP over x) on `threads` host
+    threads, on a bounded sample of the workload: whole 4096^2 time steps, as many as fit the
+    budget after one warm-up step."""
+    from oracle import oracle as O
+    p, cm, bcs, f, dt = oracle_channel(O, tau_s)
     t0 = time.perf_counter()
-    f = O.run("D2Q9", p, cm, bcs, f, 0, 0, dt=sc["delta_t"], nthreads=threads)
+    f = O.run("D2Q9", p, cm, bcs, f, 0, 0, dt=dt, nthreads=threads)
     one = time.perf_counter() - t0
     n = max(1, min(50, int(budget_s / max(one, 1e-3))))
     t0 = time.perf_counter()
-    O.run("D2Q9", p, cm, bcs, f, 1, n, dt=sc["delta_t"], nthreads=threads)
+    O.run("D2Q9", p, cm, bcs, f, 1, n, dt=dt, nthreads=threads)
     el = time.perf_counter() - t0
     return {"value": NX * NY * n / el / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
             "sample": f"{n} time steps of the full {NX}x{NY} lattice (after 1 warm-up step), "
-                      f"{threads} OpenMP threads, C++ restatement of the reference loop"}
+                      f"{threads} OpenMP thread{'s' if threads > 1 else ''}, C++ restatement of the reference loop"}
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline(tau_s, budget_s=12.0):
+    """The oracle port on all host cores (the reported baseline) and on one core (the reference
+    itself is single-threaded: src/ has no threading), each on a bounded sample."""
+    from oracle import oracle as O
+    threads = O.max_threads()
+    res = cpu_rate(tau_s, threads, budget_s)
+    res["single_thread"] = cpu_rate(tau_s, 1, budget_s) if threads > 1 else dict(res)
+    res["cpu"] = cpu_model()
+    return res
 
 
 def bench_tgv64(torch, lbm, storage="f64"):
@@ -375,21 +403,39 @@ def dist_setup(args):
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference loop on all host threads (the
+    reference is Julia, absent on the box), timed over exactly `--steps` steps after `--warmup`
+    untimed ones.  A step is one time step of a 4096-wide channel: the full 4096 rows when the
+    run fits a few minutes, else a strip of fewer rows (walls North / South, same τ and force),
+    so that steps x ms_per_step is the timed region."""
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return 0
     tau_s = tau_from_seed()
     from oracle import oracle as O
     O.build()
-    steps = max(1, args.steps)
-    res = cpu_baseline(tau_s, budget_s=min(120.0, 3.0 + 0.05 * steps))
-    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "MLUPS", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": NX * NY / res["value"] / 1e3,
+    threads = O.max_threads()
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
+    # ~0.4 s per full step on 16 cores: full lattice up to 100 steps in all, else fewer rows
+    ny = NY if steps + warmup <= 100 else max(64, (NY * 100 // (steps + warmup)) // 8 * 8)
+    p, cm, bcs, f, dt = oracle_channel(O, tau_s, NX, ny)
+    if warmup:
+        f = O.run("D2Q9", p, cm, bcs, f, 0, warmup - 1, dt=dt, nthreads=threads)
+    t0 = time.perf_counter()
+    O.run("D2Q9", p, cm, bcs, f, warmup, warmup + steps - 1, dt=dt, nthreads=threads)
+    el = time.perf_counter() - t0
+    value = NX * ny * steps / el / 1e6
+    sample = (f"{steps} time steps (after {warmup} untimed) of a {NX}x{ny} D2Q9 TRT channel"
+              f"{'' if ny == NY else ' (a strip of the 4096x4096 workload, same walls, tau and force)'}, "
+              f"{threads} OpenMP threads, C++ restatement of the reference loop")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warmup, "ms_per_step": el / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "D2Q9 TRT Poiseuille 4096x4096, FP64, CPU oracle port (the reference is Julia, "
-                                   "not runnable on the box)", "nx": NX, "ny": NY, "tau_s": tau_s},
-            "cpu_baseline": res,
-            "e2e": {"value": res["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": {"workload": "D2Q9 TRT Poiseuille channel, FP64, CPU oracle port (the reference is Julia, "
+                                   "not runnable on the box)", "nx": NX, "ny": ny, "tau_s": tau_s,
+                       "cpu": cpu_model()},
+            "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(finite(line), allow_nan=False))
     return 0
 
@@ -518,12 +564,13 @@ def main():
         fp64_inst = profiled_traffic().get("step_f64_fp64_thread_inst_per_lu")
         if args.storage == "f64" and fp64_inst and clocks and clocks.get("sm_mhz"):
             # the FP64 step's own roof: GB300 issues 2 FP64 thread instructions per SM per clock
-            peak = 152 * 2 * clocks["sm_mhz"] * 1e6 / 1e9
+            sms = torch.cuda.get_device_properties(local if world > 1 else 0).multi_processor_count
+            peak = sms * 2 * clocks["sm_mhz"] * 1e6 / 1e9
             ach = fp64_inst * mlups * 1e6 / 1e9
             line["compute_roofline"] = {"bound": "fp64 pipe", "achieved": ach, "peak": peak,
                                         "unit": "G FP64 thread-instructions/s", "frac": ach / peak,
                                         "instructions_per_lu": fp64_inst,
-                                        "peak_source": "152 SMs x 2 FP64 instructions per clock (rate measured with ncu) "
+                                        "peak_source": f"{sms} SMs x 2 FP64 instructions per clock (rate measured with ncu) "
                                                        "x median SM clock of the timed region"}
         line.update(extra)
         print(json.dumps(finite(line), allow_nan=False))

@@ -25,6 +25,13 @@
  *   - One context is used by one host thread at a time.  Work is issued on the context's
  *     stream (its own non-blocking stream, or the one given to lbm_set_stream); calls that
  *     return host data synchronise that stream, lbm_step does not.
+ *   - Devices: a context lives on the device that was current when lbm_create ran.  Every call on
+ *     a context (or a batch / adjoint built on it) makes that device current for its duration
+ *     and makes the caller's current device current again before it returns.
+ *     lbm_reduce_noalloc, which has no context, runs on the caller's current device.
+ *   - A failure of a CUDA call inside the library (status LBM_ERR_CUDA or LBM_ERR_NOMEM) is read
+ *     and cleared from the thread's last-error slot when it is returned; other failures leave
+ *     that slot as the caller left it.
  */
 #ifndef LBM_GB300_H
 #define LBM_GB300_H
@@ -298,7 +305,10 @@ const char* lbm_adjoint_last_error(const lbm_adjoint* adjoint);
  * that overlap on the GPU (different streams, or different host threads on one device) race on
  * it: serialise them.  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream
- * capture.  Returns LBM_OK after the launch; read `out` after synchronising `stream`. */
+ * capture.  The cached address does not survive cudaDeviceReset: do not call this entry point
+ * again in a process that reset the device.  It runs on the calling thread's current device: f,
+ * out and the analytic fields must be memory of that device (or managed memory), else
+ * LBM_ERR_INVALID.  Returns LBM_OK after the launch; read `out` after synchronising `stream`. */
 int32_t lbm_reduce_noalloc(int32_t quadrature, const double* weights, double speed_of_sound_squared, int64_t nx,
                            int64_t ny, const double* f, int32_t kind, const lbm_analytic* analytic, double* out,
                            void* stream);

@@ -125,6 +125,32 @@ namespace {
 // not report it again.  An error that corrupts the context is not dropped by this: every later
 // call returns it.
 void drop_reported_error() { (void)cudaGetLastError(); }
+// Only the statuses that report a failed CUDA call (an allocation, a copy, a launch) read and drop
+// the thread's last CUDA error; a validation failure leaves an error that the caller's own CUDA
+// code left pending for the caller to see.
+void drop_if_cuda(int status) {
+  if (status == LBM_ERR_CUDA || status == LBM_ERR_NOMEM) drop_reported_error();
+}
+
+// Makes a context's device current for the scope of an entry point and makes the caller's device
+// current again on every return, so that a call on a context of device k leaves the calling
+// thread's current device as it found it.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      prev = -1;
+      drop_reported_error();
+    }
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
 
 // Allocations that leave the pointer null when they fail, so that a destroy after a partial
 // creation frees only what was allocated.
@@ -153,7 +179,7 @@ bool make_event(cudaEvent_t* ev) {
 
 int fail(lbm_ctx* c, int status, const std::string& msg) {
   if (c) c->err = msg;
-  drop_reported_error();
+  drop_if_cuda(status);
   return status;
 }
 
@@ -335,7 +361,10 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   if (!out || !d) return LBM_ERR_INVALID;
   *out = nullptr;
   if (d->quadrature < 0 || d->quadrature > 6) return LBM_ERR_INVALID;
-  if (d->nx < 1 || d->ny < 1 || d->nx * d->ny >= (int64_t(1) << 31)) return LBM_ERR_INVALID;
+  // each factor is bounded before the product is formed, so the product cannot wrap
+  if (d->nx < 1 || d->ny < 1 || d->nx >= (int64_t(1) << 31) || d->ny >= (int64_t(1) << 31) ||
+      d->nx * d->ny >= (int64_t(1) << 31))
+    return LBM_ERR_INVALID;
   if (d->storage < 0 || d->storage > 3) return LBM_ERR_INVALID;
   if (d->collision < 0 || d->collision > 3) return LBM_ERR_INVALID;
   if (d->force_kind < 0 || d->force_kind > 3) return LBM_ERR_INVALID;
@@ -657,7 +686,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
 
 void lbm_destroy(lbm_ctx* c) {
   if (!c) return;
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_graphs(c);
   for (int k = 0; k < 2; ++k) cudaFree(c->buf[k]);
@@ -681,7 +710,7 @@ void lbm_destroy(lbm_ctx* c) {
 
 int32_t lbm_set_stream(lbm_ctx* c, void* stream) {
   if (!c) return LBM_ERR_INVALID;
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   LBM_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
   free_graphs(c);  // graphs are captured on, and launched into, a stream; recapture lazily
@@ -690,14 +719,14 @@ int32_t lbm_set_stream(lbm_ctx* c, void* stream) {
 
 int32_t lbm_synchronize(lbm_ctx* c) {
   if (!c) return LBM_ERR_INVALID;
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   LBM_CUDA(c, cudaStreamSynchronize(c->stream));
   return LBM_OK;
 }
 
 static int upload_impl(lbm_ctx* c, const double* f, cudaMemcpyKind kind) {
   if (!c || !f) return LBM_ERR_INVALID;
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   const size_t cnt = (size_t)c->n * c->Q;
   if (c->storage == LBM_STORE_F64) {
     LBM_CUDA(c, cudaMemcpyAsync(c->buf[0], f, cnt * sizeof(double), kind, c->stream));
@@ -724,7 +753,7 @@ int32_t lbm_initialize_fields(lbm_ctx* c, const double* rho, const double* ux, c
   if (!c) return LBM_ERR_INVALID;
   const bool any_s = sxx || sxy || syy, all_s = sxx && sxy && syy;
   if (any_s && !all_s) return fail(c, LBM_ERR_INVALID, "the stress tensor needs sxx, sxy and syy");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   const double* host[7] = {rho, ux, uy, T, sxx, sxy, syy};
   int nplanes = 0;
   for (const double* h : host) nplanes += h ? 1 : 0;
@@ -766,7 +795,7 @@ int32_t lbm_upload_device(lbm_ctx* c, const double* f) { return upload_impl(c, f
 static int download_impl(lbm_ctx* c, double* f, cudaMemcpyKind kind) {
   if (!c || !f) return LBM_ERR_INVALID;
   if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   const size_t cnt = (size_t)c->n * c->Q;
   if (c->storage == LBM_STORE_F64) {
     int rc = materialise(c);
@@ -793,7 +822,7 @@ int32_t lbm_download_device(lbm_ctx* c, double* f) { return download_impl(c, f, 
 int32_t lbm_step(lbm_ctx* c, int64_t nsteps, int64_t t0, double dt) {
   if (!c || nsteps < 0) return LBM_ERR_INVALID;
   if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   c->last_launches = 0;
   int64_t k = 0;
   const bool time_dependent = c->force_kind == LBM_FORCE_SHEAR;
@@ -829,7 +858,7 @@ int32_t lbm_step(lbm_ctx* c, int64_t nsteps, int64_t t0, double dt) {
 int32_t lbm_reduce(lbm_ctx* c, int32_t kind, const lbm_analytic* an, double* out) {
   if (!c || !out) return LBM_ERR_INVALID;
   if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   if ((!c->d_partial && !dev_malloc(&c->d_partial, (size_t)c->red_blocks * kRedMaxK * sizeof(double))) ||
       (!c->d_out && !dev_malloc(&c->d_out, kRedMaxK * sizeof(double))) ||
       (!c->h_out && !host_malloc(&c->h_out, kRedMaxK * sizeof(double))))
@@ -920,7 +949,7 @@ int32_t lbm_reduce(lbm_ctx* c, int32_t kind, const lbm_analytic* an, double* out
 int32_t lbm_macroscopic(lbm_ctx* c, double* rho, double* ux, double* uy) {
   if (!c) return LBM_ERR_INVALID;
   if (!c->have_state) return fail(c, LBM_ERR_STATE, "no state uploaded");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   int rc = ensure(c, &c->d_macro, (size_t)c->n * 3 * sizeof(double));
   if (rc) return rc;
   OpArgs a = base_args(c, OP_MACRO);
@@ -941,7 +970,7 @@ int32_t lbm_macroscopic(lbm_ctx* c, double* rho, double* ux, double* uy) {
 int32_t lbm_collide_device(lbm_ctx* c, const double* f_in, double* f_out, double time) {
   if (!c || !f_in || !f_out) return LBM_ERR_INVALID;
   if (c->storage != LBM_STORE_F64) return fail(c, LBM_ERR_UNSUPPORTED, "device operators need FP64 storage");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   set_time(c, time);
   OpArgs a = base_args(c, OP_COLLIDE);
   a.src = f_in;
@@ -952,7 +981,7 @@ int32_t lbm_collide_device(lbm_ctx* c, const double* f_in, double* f_out, double
 int32_t lbm_stream_device(lbm_ctx* c, const double* f, double* f_new) {
   if (!c || !f || !f_new) return LBM_ERR_INVALID;
   if (c->storage != LBM_STORE_F64) return fail(c, LBM_ERR_UNSUPPORTED, "device operators need FP64 storage");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   OpArgs a = base_args(c, OP_STREAM);
   a.src = f;
   a.dst = f_new;
@@ -962,7 +991,7 @@ int32_t lbm_stream_device(lbm_ctx* c, const double* f, double* f_new) {
 int32_t lbm_apply_bcs_device(lbm_ctx* c, double* f_new, const double* f_old) {
   if (!c || !f_new || !f_old) return LBM_ERR_INVALID;
   if (c->storage != LBM_STORE_F64) return fail(c, LBM_ERR_UNSUPPORTED, "device operators need FP64 storage");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   if (c->pd.nbc == 0) return LBM_OK;
   OpArgs a = base_args(c, OP_APPLY_BC);
   a.src = f_old;
@@ -1013,7 +1042,7 @@ namespace {
 
 int bfail(lbm_batch* b, int status, const std::string& msg) {
   if (b) b->err = msg;
-  drop_reported_error();
+  drop_if_cuda(status);
   return status;
 }
 
@@ -1087,7 +1116,7 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
   b->device = c0->device;
   b->storage = c0->storage;
   b->coll = c0->coll;
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   const size_t sb = batch_static_size(b->storage);
   std::vector<char> h(sb * count);
   for (int k = 0; k < count; ++k) {
@@ -1115,7 +1144,7 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
 
 void lbm_batch_destroy(lbm_batch* b) {
   if (!b) return;
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->shared)
     for (lbm_ctx* c : b->members)
@@ -1145,7 +1174,7 @@ int64_t lbm_batch_last_launch_count(const lbm_batch* b) { return b ? b->last_lau
 
 int32_t lbm_batch_set_stream(lbm_batch* b, void* stream) {
   if (!b) return LBM_ERR_INVALID;
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "stream synchronize");
   cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
   if (b->shared)
@@ -1165,7 +1194,7 @@ int32_t lbm_batch_set_stream(lbm_batch* b, void* stream) {
 // back when the batch is destroyed.
 int32_t lbm_batch_share_stream(lbm_batch* b) {
   if (!b) return LBM_ERR_INVALID;
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   for (lbm_ctx* c : b->members) {
     if (c->stream == b->stream) continue;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "member synchronize");
@@ -1177,7 +1206,7 @@ int32_t lbm_batch_share_stream(lbm_batch* b) {
 
 int32_t lbm_batch_synchronize(lbm_batch* b) {
   if (!b) return LBM_ERR_INVALID;
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   return cudaStreamSynchronize(b->stream) == cudaSuccess ? LBM_OK : bfail(b, LBM_ERR_CUDA, "synchronize");
 }
 
@@ -1190,7 +1219,7 @@ namespace {
 // One call of lbm_batch_step(_timed): t0 / dt (member order) give each member's time index at its
 // first step and its time step, or are null for members whose forces do not depend on time.
 int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, const double* dt) {
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   const int count = (int)b->members.size();
   for (int k = 0; k < count; ++k) {
     if (nsteps[k] < 0) return bfail(b, LBM_ERR_INVALID, "negative step count");
@@ -1422,7 +1451,7 @@ int32_t lbm_batch_reduce(lbm_batch* b, int32_t kind, const uint8_t* select, doub
   if (!b || !out) return LBM_ERR_INVALID;
   if (kind != LBM_REDUCE_MEAN_VELOCITY && kind != LBM_REDUCE_VELOCITY_CONVERGENCE && kind != LBM_REDUCE_CONSERVED)
     return bfail(b, LBM_ERR_UNSUPPORTED, "batched reductions: MEAN_VELOCITY, VELOCITY_CONVERGENCE, CONSERVED");
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   const int count = (int)b->members.size();
   std::vector<int> selected;
   for (int k = 0; k < count; ++k)
@@ -1446,7 +1475,7 @@ int32_t lbm_batch_reduce_fields(lbm_batch* b, int32_t kind, const uint8_t* selec
   if (!b || !out || !analytic) return LBM_ERR_INVALID;
   if (kind != LBM_REDUCE_TRACK_ERRORS && kind != LBM_REDUCE_COMPARE)
     return bfail(b, LBM_ERR_UNSUPPORTED, "batched field reductions: TRACK_ERRORS, COMPARE");
-  cudaSetDevice(b->device);
+  DeviceGuard device_guard(b->device);
   const int count = (int)b->members.size();
   const int need = kind == LBM_REDUCE_TRACK_ERRORS ? 8 : 4;
   std::vector<int> selected;
@@ -1546,7 +1575,7 @@ namespace {
 
 int afail(lbm_adjoint* a, int status, const std::string& msg) {
   if (a) a->err = msg;
-  drop_reported_error();
+  drop_if_cuda(status);
   return status;
 }
 
@@ -1641,7 +1670,7 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
   if (c->pd.nbc != 0) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: periodic lattices only");
   if (c->force_kind != LBM_FORCE_NONE && c->force_kind != LBM_FORCE_CONSTANT)
     return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: uniform force only");
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   lbm_adjoint* a = new lbm_adjoint();
   a->ctx = c;
   a->T = nsteps;
@@ -1673,7 +1702,7 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
 
 void lbm_adjoint_destroy(lbm_adjoint* a) {
   if (!a) return;
-  cudaSetDevice(a->ctx->device);
+  DeviceGuard device_guard(a->ctx->device);
   cudaStreamSynchronize(a->ctx->stream);
   if (a->graph) cudaGraphExecDestroy(a->graph);
   void* bufs[] = {a->a0, a->fwd[0], a->fwd[1], a->lam[0], a->lam[1], a->d_u0, a->d_ut, a->d_grad, a->d_slots, a->d_out};
@@ -1690,7 +1719,7 @@ int32_t lbm_adjoint_run(lbm_adjoint* a, const double* u0, const double* u_target
                         double* grad_u0) {
   if (!a || !u0 || !u_target || !result) return LBM_ERR_INVALID;
   lbm_ctx* c = a->ctx;
-  cudaSetDevice(c->device);
+  DeviceGuard device_guard(c->device);
   cudaStream_t s = c->stream;
   const size_t vb = (size_t)c->n * 2 * sizeof(double);
   if (cudaMemcpyAsync(a->d_u0, u0, vb, cudaMemcpyDefault, s) != cudaSuccess ||

@@ -153,7 +153,7 @@ __device__ __forceinline__ void acc_add(CT& v, bool& set, CT t) {
 // offset of the unrolled per-population loops folds to a register or an immediate.
 //   R     : largest |c| component (halo radius of the pull)
 //   EQ    : truncation order of `equilibrium!` (velocity_distribution_function/*.jl)
-//   HN    : Hermite order of the regularised MRT, div(order(q), 2) (mrt.jl:147)
+//   HN    : Hermite order of the regularised MRT, div(order(q), 2) (mrt.jl:68)
 // ---------------------------------------------------------------------------------------
 #define LBM_DEFINE_LATTICE(NAME, ID, QQ, RR, EQQ, HNN, CXS, CYS, OPS)                    \
   struct NAME {                                                                           \

@@ -14,6 +14,9 @@
 // bytes until the process exits.  Host code cannot use the name of the array as a device
 // address (it names a host-side stand-in), so each device's address is looked up once with
 // cudaGetSymbolAddress, with that device current, the first time the entry point runs on it.
+// The cached address belongs to the device's context: it does not survive cudaDeviceReset (or
+// any other teardown of the primary context), after which this entry point must not be called
+// again in the process.
 //
 // Reductions run in the same kernels, grid size and fixed block order as lbm_reduce, so for
 // the same populations the two entry points return the same sums.
@@ -50,6 +53,19 @@ cudaError_t scratch_address(double** out) {
   return cudaSuccess;
 }
 
+// The kernel runs on the current device, so every array it reads or writes must be memory of that
+// device: a pointer into another GPU's memory, or into host memory the runtime does not know, is
+// refused before the launch (cudaPointerGetAttributes allocates nothing).
+bool on_device(const void* ptr, int dev) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  if (at.type == cudaMemoryTypeDevice) return at.device == dev;
+  return at.type == cudaMemoryTypeManaged;
+}
+
 typedef cudaError_t (*RunFn)(const lbm::OpArgs&);
 const RunFn kRunNoAlloc[7] = {lbm::run_op_q4, lbm::run_op_q5, lbm::run_op_q9, lbm::run_op_q13,
                               lbm::run_op_q17, lbm::run_op_q21, lbm::run_op_q37};
@@ -62,7 +78,9 @@ extern "C" int32_t lbm_reduce_noalloc(int32_t quadrature, const double* weights,
   using namespace lbm;
   if (quadrature < 0 || quadrature > 6 || !weights || !f || !out) return LBM_ERR_INVALID;
   // The node index is a 32-bit integer: lattices of 2^31 nodes or more are rejected.
-  if (nx < 1 || ny < 1 || nx * ny >= (int64_t(1) << 31)) return LBM_ERR_INVALID;
+  // Each factor is bounded first, so the product below cannot wrap.
+  if (nx < 1 || ny < 1 || nx >= (int64_t(1) << 31) || ny >= (int64_t(1) << 31) || nx * ny >= (int64_t(1) << 31))
+    return LBM_ERR_INVALID;
   int K = 0;
   switch (kind) {
     case LBM_REDUCE_TRACK_ERRORS: K = 16; break;
@@ -81,6 +99,19 @@ extern "C" int32_t lbm_reduce_noalloc(int32_t quadrature, const double* weights,
   const int64_t n = nx * ny;
   const int nblocks = (int)std::min<int64_t>((n + kRedThreads - 1) / kRedThreads, kNoAllocBlocks);
   if ((int64_t)nblocks * K > kNoAllocSlots) return LBM_ERR_INVALID;
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return LBM_ERR_CUDA;
+  }
+  if (!on_device(f, dev) || !on_device(out, dev)) return LBM_ERR_INVALID;
+  if (kind == LBM_REDUCE_TRACK_ERRORS || kind == LBM_REDUCE_COMPARE) {
+    const double* fields[8] = {analytic->rho, analytic->ux, analytic->uy, analytic->p,
+                               analytic->sxx, analytic->syx, analytic->sxy, analytic->syy};
+    for (int k = 0; k < (kind == LBM_REDUCE_TRACK_ERRORS ? 8 : 4); ++k)
+      if (!on_device(fields[k], dev)) return LBM_ERR_INVALID;
+  }
 
   double* scratch = nullptr;
   if (scratch_address(&scratch) != cudaSuccess) {

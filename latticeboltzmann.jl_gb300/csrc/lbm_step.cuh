@@ -353,7 +353,7 @@ __device__ __forceinline__ void mrt_accumulate_quad(CT* M, bool* set, CT fpp, CT
   });
 }
 
-// Regularised MRT collision on one node (mrt.jl:135-197), written with raw moments: the
+// Regularised MRT collision on one node (mrt.jl:56-118), written with raw moments: the
 // Hermite coefficients a_f^(n) = Σ f_i H_n(c_i) of orders 2..N are formed from the raw
 // moments M_ab, relaxed towards a_eq^(n) = ρ u^{⊗n}, and the populations are rebuilt as
 // w_i (ρ + cs ρ u·c_i + Σ_n cs^n / n! a_coll^(n) : H_n(c_i)), expanded in monomials of c_i.

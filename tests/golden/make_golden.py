@@ -6,7 +6,10 @@
    VelocityConvergenceStoppingCriteria(1e-7).  Parsed from the notebook's JSON (read here
    from the reference checkout given on the command line); the values are the reference's
    own printed output, rounded to 6 significant digits by its DataFrame display.
-2. oracle_vectors.json -- outputs of the CPU oracle on small inputs (populations after a few
+2. trt_magic_parameter_table.json -- the 30 rows of the same cell's HTML table, which prints all
+   seven columns of the results, including error_σ_xx (Inf in every row: the analytic σ_xx of the
+   channel is zero, so its relative error divides by zero) and error_σ_xy.
+3. oracle_vectors.json -- outputs of the CPU oracle on small inputs (populations after a few
    steps and error-norm rows), so that the oracle built on another machine can be checked
    against the one that was validated here.
 
@@ -36,6 +39,26 @@ def notebook_rows(ref_root):
         if rows:
             break
     return rows
+
+
+def notebook_table(ref_root):
+    """The HTML DataFrame table of the same output: <tr><th>k</th><td>τ_s</td><td>τ_a</td>
+    <td>"D2Q9"</td><td>error_u</td><td>error_p</td><td>error_σ_xx</td><td>error_σ_xy</td></tr>."""
+    nb = json.load(open(os.path.join(ref_root, "examples", "notebooks", "trt_magic_parameter.ipynb")))
+    keys = ["tau_s", "tau_a", "quadrature", "error_u", "error_p", "error_sigma_xx", "error_sigma_xy"]
+    for cell in nb["cells"]:
+        for out in cell.get("outputs", []):
+            html = "".join(out.get("data", {}).get("text/html", ""))
+            rows = []
+            for m in re.finditer(r"<tr><th>(\d+)</th>((?:<td>[^<]*</td>){7})</tr>", html):
+                cells = re.findall(r"<td>([^<]*)</td>", m.group(2))
+                row = {"row": int(m.group(1))}
+                for k, v in zip(keys, cells):
+                    row[k] = v.strip('"') if k == "quadrature" else v  # numbers kept as printed ("Inf")
+                rows.append(row)
+            if rows:
+                return rows
+    return []
 
 
 def oracle_vectors():
@@ -74,5 +97,10 @@ if __name__ == "__main__":
     assert len(rows) == 21, len(rows)
     json.dump({"source": "examples/notebooks/trt_magic_parameter.ipynb, cell 2 output", "rows": rows},
               open(os.path.join(HERE, "trt_magic_parameter_rows.json"), "w"), indent=1)
+    table = notebook_table(ref)
+    assert len(table) == 30, len(table)
+    json.dump({"source": "examples/notebooks/trt_magic_parameter.ipynb, cell 2 output (HTML table)",
+               "note": "values as printed (6 significant digits); error_sigma_xx is the string Inf",
+               "rows": table}, open(os.path.join(HERE, "trt_magic_parameter_table.json"), "w"), indent=1)
     json.dump(oracle_vectors(), open(os.path.join(HERE, "oracle_vectors.json"), "w"), indent=1)
-    print("wrote", len(rows), "notebook rows and the oracle vectors")
+    print("wrote", len(rows), "notebook rows,", len(table), "table rows and the oracle vectors")

@@ -113,3 +113,22 @@ def test_null_handles(lbm, L):
     assert L.lbm_batch_reduce(None, 2, None, out.ctypes.data_as(N._DP)) == N.LBM_ERR_INVALID
     assert L.lbm_batch_last_error(None).decode() == "null batch"
     L.lbm_batch_destroy(None)
+
+
+@pytest.mark.parametrize("nx,ny", [(2 ** 62 + 1, 4), (4, 2 ** 62 + 1), (2 ** 31, 1), (1, 2 ** 31),
+                                   (2 ** 16, 2 ** 15)])
+def test_lattice_sizes_that_wrap_or_exceed_32_bit_node_indices(lbm, L, nx, ny):
+    """nx * ny formed in 64 bits wraps for (2^62 + 1) x 4 to 4 nodes; each factor is bounded
+    before the product, so such pairs are refused like every lattice of 2^31 nodes or more."""
+    N = lbm._native
+    assert _create(L, _desc(lbm, nx=nx, ny=ny)) == N.LBM_ERR_INVALID
+    q = lbm.D2Q9()
+    w = np.asarray(q.weights, dtype=np.float64)
+    fn = L.lbm_reduce_noalloc
+    fn.argtypes = [C.c_int32, C.POINTER(C.c_double), C.c_double, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
+                   C.POINTER(N.LbmAnalytic), C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int32
+    dummy = np.zeros(16)  # never read: the sizes are refused before any pointer is used
+    st = fn(q.qid, w.ctypes.data_as(C.POINTER(C.c_double)), q.speed_of_sound_squared, nx, ny,
+            dummy.ctypes.data, N.REDUCE_CONSERVED, None, dummy.ctypes.data, None)
+    assert st == N.LBM_ERR_INVALID

@@ -12,6 +12,7 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROWS = json.load(open(os.path.join(HERE, "golden", "trt_magic_parameter_rows.json")))["rows"]
+TABLE = json.load(open(os.path.join(HERE, "golden", "trt_magic_parameter_table.json")))["rows"]
 
 
 def test_batched_sweep_reproduces_the_notebook_rows(lbm_gpu):
@@ -24,6 +25,22 @@ def test_batched_sweep_reproduces_the_notebook_rows(lbm_gpu):
         last = m.processing_method.df[-1]
         assert last.error_u == pytest.approx(r["error_u"], rel=6e-6), r
         assert last.error_p == pytest.approx(r["error_p"], rel=6e-6), r
+        m.close()
+
+
+def test_batched_sweep_reproduces_the_notebook_table(lbm_gpu):
+    """The notebook's 30-row HTML table as ONE batch, every printed column: error_u, error_p and
+    error_σ_xy to the printed digits, error_σ_xx = Inf (zero analytic σ_xx)."""
+    lbm = lbm_gpu
+    points = [(float(r["tau_s"]), float(r["tau_a"])) for r in TABLE]
+    models, times = lbm.build_trt_sweep_models(points, scale=1)
+    lbm.simulate_batch(models, times)
+    for r, m in zip(TABLE, models):
+        last = m.processing_method.df[-1]
+        assert last.error_u == pytest.approx(float(r["error_u"]), rel=6e-6), r
+        assert last.error_p == pytest.approx(float(r["error_p"]), rel=6e-6), r
+        assert last.error_σ_xy == pytest.approx(float(r["error_sigma_xy"]), rel=6e-6), r
+        assert r["error_sigma_xx"] == "Inf" and last.error_σ_xx == float("inf"), r
         m.close()
 
 

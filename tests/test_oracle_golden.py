@@ -9,6 +9,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROWS = json.load(open(os.path.join(HERE, "golden", "trt_magic_parameter_rows.json")))["rows"]
 VECS = json.load(open(os.path.join(HERE, "golden", "oracle_vectors.json")))
+TABLE = json.load(open(os.path.join(HERE, "golden", "trt_magic_parameter_table.json")))["rows"]
 
 
 def _poiseuille_row(O, tau_s, tau_a):
@@ -31,6 +32,19 @@ def test_oracle_reproduces_reference_notebook_rows(O, row):
     # the notebook prints 6 significant digits
     assert r["error_u"] == pytest.approx(row["error_u"], rel=6e-6)
     assert r["error_p"] == pytest.approx(row["error_p"], rel=6e-6)
+
+
+@pytest.mark.parametrize("row", TABLE, ids=[f"{r['tau_s']}-{r['tau_a']}" for r in TABLE])
+def test_oracle_reproduces_reference_table_rows(O, row):
+    """The notebook's 30-row HTML table, every printed column: error_u, error_p and error_σ_xy to
+    the 6 printed digits, and error_σ_xx = Inf (the channel's analytic σ_xx is zero, and the
+    reference divides by its norm, track_hydrodynamic_errors.jl:176-187)."""
+    r = _poiseuille_row(O, float(row["tau_s"]), float(row["tau_a"]))
+    assert row["quadrature"] == "D2Q9"
+    assert r["error_u"] == pytest.approx(float(row["error_u"]), rel=6e-6)
+    assert r["error_p"] == pytest.approx(float(row["error_p"]), rel=6e-6)
+    assert r["error_sigma_xy"] == pytest.approx(float(row["error_sigma_xy"]), rel=6e-6)
+    assert row["error_sigma_xx"] == "Inf" and r["error_sigma_xx"] == float("inf")
 
 
 def test_oracle_vectors(O):
