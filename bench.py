@@ -195,13 +195,21 @@ def cpu_rate(tau_s, threads, budget_s):
 
 
 def cpu_model():
+    """The host CPU's model name (lscpu), else what /proc/cpuinfo or the platform gives."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return f"{line.split(':', 1)[1].strip()} ({platform.machine()})"
+    except Exception:
+        pass
     try:
         for line in open("/proc/cpuinfo"):
             if line.lower().startswith(("model name", "cpu part")):
-                return line.split(":", 1)[1].strip()
+                return f"{line.split(':', 1)[1].strip()} ({platform.machine()})"
     except Exception:
         pass
-    import platform
     return platform.processor() or platform.machine()
 
 

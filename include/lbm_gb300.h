@@ -259,6 +259,23 @@ int32_t lbm_batch_reduce(lbm_batch* batch, int32_t kind, const uint8_t* select, 
  * members not selected are not read); out as for lbm_batch_reduce.  Synchronous. */
 int32_t lbm_batch_reduce_fields(lbm_batch* batch, int32_t kind, const uint8_t* select, const lbm_analytic* analytic,
                                 double* out);
+/* Block-resident stepping of small members (no counterpart in the reference, which steps each
+ * lattice in its own `simulate`).  Per velocity set q (lbm_quadrature index):
+ *   resident_max_nodes[q]  members of at most this many nodes take ALL their steps of a
+ *                          lbm_batch_step(_timed) call in one kernel launch, their populations held
+ *                          in shared memory (0: never; such members use the graph path);
+ *   nodes_per_block[q]     nodes per CTA: a resident member runs on a thread-block cluster of
+ *                          ceil(n / nodes_per_block[q]) CTAs, rounded up to a power of two, at
+ *                          most 8, the pull crossing CTAs through distributed shared memory.
+ * A member whose share of both population buffers would not fit one CTA's shared memory takes the
+ * graph path.  Results are the same bits on either path (same populations, same collision
+ * arithmetic).  lbm_batch_set_schedule(batch, NULL) puts every member on the graph path, the
+ * state of a new batch.  The Python binding sets a schedule measured on the GPU. */
+typedef struct {
+  int64_t resident_max_nodes[7];
+  int32_t nodes_per_block[7];
+} lbm_batch_schedule;
+int32_t lbm_batch_set_schedule(lbm_batch* batch, const lbm_batch_schedule* schedule);
 /* Members issue their own calls on the batch's stream until the batch is destroyed (no ordering
  * between streams per batch call; members must outlive the batch). */
 int32_t lbm_batch_share_stream(lbm_batch* batch);

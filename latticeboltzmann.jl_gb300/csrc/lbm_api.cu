@@ -15,7 +15,7 @@
 #include <vector>
 
 #include "lbm_ops.cuh"
-#include "lbm_batch.cuh"
+#include "lbm_resident.cuh"
 #include "lbm_adjoint.cuh"
 
 using namespace lbm;
@@ -27,6 +27,8 @@ cudaError_t batch_reduce_launch(int storage, int qid, int K, const void* statics
                                 const BatchDyn* dyn, int nmem, long long blocks, double* partial, long long part_base,
                                 double* out, cudaStream_t s);
 size_t batch_static_size(int storage);
+cudaError_t resident_launch(int storage, int coll, int qid, const void* statics, const ResidentDyn* dyn, int nmem,
+                            int csize, int stride, int threads, cudaStream_t s);
 struct AdjArgs;
 cudaError_t adj_launch(int op, int qid, int storage, int coll, const void* params, AdjArgs a, const void* src, int pull,
                        const void* lam_next, void* lam_out, double* slots, int nblocks, const double* u0,
@@ -1012,6 +1014,15 @@ struct lbm_batch {
   BatchDyn* d_dyn = nullptr;      // per call, launch order
   BatchDyn* h_dyn = nullptr;      // pinned staging copy
   cudaEvent_t staged = nullptr;   // the last upload from h_dyn has completed
+  // block-resident members (lbm_resident.cuh): the schedule, the per-call descriptors (staged
+  // with h_dyn) and one stream + event per resident launch, forked from and joined to `stream`
+  lbm_batch_schedule schedule{};  // zero: every member on the graph path
+  ResidentDyn* d_rdyn = nullptr;
+  ResidentDyn* h_rdyn = nullptr;
+  std::vector<cudaStream_t> res_streams;
+  std::vector<cudaEvent_t> res_events;
+  cudaEvent_t res_fork = nullptr;
+  int64_t res_launches = 0;
   ReduceArgs* d_rargs = nullptr;  // per member, set up by the first reduction
   std::vector<ReduceArgs> h_rargs; // host copy of the same
   ReduceArgs* d_rargs_call = nullptr;  // per member, with this call's analytic fields
@@ -1080,14 +1091,36 @@ int batch_release_members(lbm_batch* b) {
 
 // Uploads dyn[0..count) through the pinned staging buffer (waiting for the previous upload from
 // it to finish before it is overwritten).
-int batch_upload_dyn(lbm_batch* b, const std::vector<BatchDyn>& dyn) {
+int batch_upload_dyn(lbm_batch* b, const std::vector<BatchDyn>& dyn, const std::vector<ResidentDyn>& rdyn) {
   if (cudaEventSynchronize(b->staged) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "staging wait");
   std::copy(dyn.begin(), dyn.end(), b->h_dyn);
+  std::copy(rdyn.begin(), rdyn.end(), b->h_rdyn);
   if (cudaMemcpyAsync(b->d_dyn, b->h_dyn, sizeof(BatchDyn) * dyn.size(), cudaMemcpyHostToDevice, b->stream) !=
           cudaSuccess ||
+      (!rdyn.empty() && cudaMemcpyAsync(b->d_rdyn, b->h_rdyn, sizeof(ResidentDyn) * rdyn.size(),
+                                        cudaMemcpyHostToDevice, b->stream) != cudaSuccess) ||
       cudaEventRecord(b->staged, b->stream) != cudaSuccess)
     return bfail(b, LBM_ERR_CUDA, "descriptor upload");
   return LBM_OK;
+}
+
+// Bytes of one population (both buffers) of a node in the batch's storage.
+size_t storage_bytes(int storage) {
+  return storage == LBM_STORE_F32_DEV ? 4 : 8;
+}
+
+// The cluster size of a block-resident member of n nodes, or 0 when the member takes the graph
+// path: at most resident_max_nodes[q] nodes, ceil(n / nodes_per_block[q]) CTAs rounded up to a
+// power of two (at most 8), and both buffers of a CTA's share within one CTA's shared memory.
+int resident_cluster(const lbm_batch* b, const lbm_ctx* c) {
+  const int64_t lim = b->schedule.resident_max_nodes[c->qid];
+  const int per = b->schedule.nodes_per_block[c->qid];
+  if (lim <= 0 || per <= 0 || c->n > lim) return 0;
+  int csize = 1;
+  while (csize < kResidentMaxCluster && (int64_t)csize * per < c->n) csize *= 2;
+  const int64_t chunk = (c->n + csize - 1) / csize;
+  if (2 * (size_t)c->Q * (size_t)chunk * storage_bytes(b->storage) > kResidentMaxSmem) return 0;
+  return csize;
 }
 
 }  // namespace
@@ -1130,6 +1163,8 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
       !dev_malloc(&b->d_static, sb * count) ||
       !dev_malloc((void**)&b->d_dyn, sizeof(BatchDyn) * count) ||
       !host_malloc((void**)&b->h_dyn, sizeof(BatchDyn) * count) ||
+      !dev_malloc((void**)&b->d_rdyn, sizeof(ResidentDyn) * count) ||
+      !host_malloc((void**)&b->h_rdyn, sizeof(ResidentDyn) * count) ||
       !dev_malloc((void**)&b->d_rout, sizeof(double) * kRedMaxK * count) ||
       !host_malloc((void**)&b->h_rout, sizeof(double) * kRedMaxK * count) ||
       cudaMemcpy(b->d_static, h.data(), sb * count, cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -1152,6 +1187,11 @@ void lbm_batch_destroy(lbm_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   cudaFree(b->d_static);
   cudaFree(b->d_dyn);
+  cudaFree(b->d_rdyn);
+  if (b->h_rdyn) cudaFreeHost(b->h_rdyn);
+  for (cudaEvent_t e : b->res_events) cudaEventDestroy(e);
+  if (b->res_fork) cudaEventDestroy(b->res_fork);
+  for (cudaStream_t st : b->res_streams) cudaStreamDestroy(st);
   cudaFree(b->d_rargs);
   cudaFree(b->d_rargs_call);
   cudaFree(b->d_ranal);
@@ -1204,6 +1244,19 @@ int32_t lbm_batch_share_stream(lbm_batch* b) {
   return LBM_OK;
 }
 
+int32_t lbm_batch_set_schedule(lbm_batch* b, const lbm_batch_schedule* schedule) {
+  if (!b) return LBM_ERR_INVALID;
+  if (!schedule) {
+    b->schedule = lbm_batch_schedule{};
+    return LBM_OK;
+  }
+  for (int q = 0; q < 7; ++q)
+    if (schedule->resident_max_nodes[q] < 0 || schedule->nodes_per_block[q] < 0)
+      return bfail(b, LBM_ERR_INVALID, "schedule: negative limit");
+  b->schedule = *schedule;
+  return LBM_OK;
+}
+
 int32_t lbm_batch_synchronize(lbm_batch* b) {
   if (!b) return LBM_ERR_INVALID;
   DeviceGuard device_guard(b->device);
@@ -1225,13 +1278,51 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
     if (nsteps[k] < 0) return bfail(b, LBM_ERR_INVALID, "negative step count");
     if (!b->members[k]->have_state) return bfail(b, LBM_ERR_STATE, "member without uploaded state");
   }
-  // members grouped by velocity set, each group in descending step order: the running set of a
-  // group at global step t is a prefix of it, with block offsets counted within the group
+  // Members that the schedule makes block-resident take all their steps in one launch per
+  // (velocity set, cluster size); the others take the graph path with the step counts below.
+  std::vector<int> csize(count, 0);
+  std::vector<int64_t> gsteps(nsteps, nsteps + count);
+  for (int k = 0; k < count; ++k)
+    if (nsteps[k] > 0 && (csize[k] = resident_cluster(b, b->members[k])) > 0) gsteps[k] = 0;
+  struct ResidentGroup {
+    int qid, csize, first, nmem, stride;
+  };
+  std::vector<ResidentDyn> rdyn;
+  std::vector<ResidentGroup> rgroups;
+  {
+    std::vector<int> res;
+    for (int k = 0; k < count; ++k)
+      if (csize[k] > 0) res.push_back(k);
+    std::stable_sort(res.begin(), res.end(), [&](int a, int c) {
+      const int qa = b->members[a]->qid, qc = b->members[c]->qid;
+      return qa != qc ? qa < qc : csize[a] < csize[c];
+    });
+    for (size_t r = 0; r < res.size(); ++r) {
+      const int k = res[r];
+      const lbm_ctx* c = b->members[k];
+      if (rgroups.empty() || rgroups.back().qid != c->qid || rgroups.back().csize != csize[k])
+        rgroups.push_back({c->qid, csize[k], (int)r, 0, 0});
+      ResidentGroup& g = rgroups.back();
+      ResidentDyn d{};
+      d.member = k;
+      d.cur0 = c->cur;
+      d.phase0 = c->phase == POST_COLLIDE ? 1 : 0;
+      d.chunk = (int)((c->n + csize[k] - 1) / csize[k]);
+      d.steps = nsteps[k];
+      d.t0 = t0 ? (long long)t0[k] : 0;
+      d.dt = dt ? dt[k] : 0.0;
+      rdyn.push_back(d);
+      g.nmem += 1;
+      g.stride = std::max(g.stride, d.chunk);
+    }
+  }
+  // graph members grouped by velocity set, each group in descending step order: the running set of
+  // a group at global step t is a prefix of it, with block offsets counted within the group
   std::vector<int> order(count);
   for (int k = 0; k < count; ++k) order[k] = k;
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
     const int qa = b->members[a]->qid, qc = b->members[c]->qid;
-    return qa != qc ? qa < qc : nsteps[a] > nsteps[c];
+    return qa != qc ? qa < qc : gsteps[a] > gsteps[c];
   });
   std::vector<int64_t> key(count);
   std::vector<long long> end(count, 0);  // end of each member's block range in its group
@@ -1239,7 +1330,7 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
   std::vector<BatchDyn> dyn(count);
   for (int r = 0; r < count; ++r) {
     const lbm_ctx* c = b->members[order[r]];
-    key[r] = nsteps[order[r]];
+    key[r] = gsteps[order[r]];
     const bool first = r == 0 || b->members[order[r - 1]]->qid != c->qid;
     if (first) group_begin.push_back(r);
     BatchDyn& d = dyn[r];
@@ -1257,11 +1348,38 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
   int64_t tmax = 0;
   for (int r = 0; r < count; ++r) tmax = std::max(tmax, key[r]);
   b->last_launches = 0;
-  if (tmax == 0) return LBM_OK;
+  if (tmax == 0 && rgroups.empty()) return LBM_OK;
   int rc = batch_wait_members(b);
   if (rc) return rc;
-  rc = batch_upload_dyn(b, dyn);
+  rc = batch_upload_dyn(b, dyn, rdyn);
   if (rc) return rc;
+  if (!rgroups.empty()) {  // resident launches on their own streams, concurrent with the graph
+    if (!b->res_fork && !make_event(&b->res_fork)) return bfail(b, LBM_ERR_CUDA, "event");
+    while (b->res_streams.size() < rgroups.size()) {
+      cudaStream_t st = nullptr;
+      if (!make_stream(&st)) return bfail(b, LBM_ERR_CUDA, "resident stream");
+      b->res_streams.push_back(st);
+    }
+    while (b->res_events.size() < rgroups.size()) {
+      cudaEvent_t ev = nullptr;
+      if (!make_event(&ev)) return bfail(b, LBM_ERR_CUDA, "resident event");
+      b->res_events.push_back(ev);
+    }
+    if (cudaEventRecord(b->res_fork, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "resident fork");
+    for (size_t gi = 0; gi < rgroups.size(); ++gi) {
+      const ResidentGroup& g = rgroups[gi];
+      cudaStream_t st = b->res_streams[gi];
+      const int threads = std::min(kResidentThreads, (g.stride + 31) / 32 * 32);
+      cudaError_t e = cudaStreamWaitEvent(st, b->res_fork, 0);
+      if (e == cudaSuccess)
+        e = resident_launch(b->storage, b->coll, g.qid, b->d_static, b->d_rdyn + g.first, g.nmem, g.csize, g.stride,
+                            threads, st);
+      if (e == cudaSuccess) e = cudaEventRecord(b->res_events[gi], st);
+      if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(e));
+    }
+  }
+  b->res_launches = (int64_t)rgroups.size();
+  if (tmax > 0) {
   if (!b->graph || b->graph_key != key || b->graph_order != order) {
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);
@@ -1325,6 +1443,11 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
   }
   if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "graph launch");
   b->last_launches = b->graph_launches;
+  }  // tmax > 0
+  for (size_t gi = 0; gi < rgroups.size(); ++gi)  // join the resident launches
+    if (cudaStreamWaitEvent(b->stream, b->res_events[gi], 0) != cudaSuccess)
+      return bfail(b, LBM_ERR_CUDA, "resident join");
+  b->last_launches += b->res_launches;
   // members continue after the batch: advance their parity / phase and order their streams
   for (int k = 0; k < count; ++k) {
     lbm_ctx* c = b->members[k];
@@ -1420,7 +1543,7 @@ int batch_reduce_run(lbm_batch* b, int K, const std::vector<int>& selected, cons
     }
     b->rpartial_blocks = total;
   }
-  int rc = batch_upload_dyn(b, dyn);
+  int rc = batch_upload_dyn(b, dyn, {});
   if (rc) return rc;
   for (size_t gi = 0; gi + 1 < group_begin.size(); ++gi) {
     const int g0 = group_begin[gi], n = group_begin[gi + 1] - g0;

@@ -230,13 +230,18 @@ class DeviceLattice:
 
 
 class DeviceBatch:
-    """Several DeviceLattices advanced together: member k takes nsteps[k] steps, all issued as one
-    CUDA graph with one kernel per global step over every member still running (lbm_batch_*).
-    Members must share storage (f64, df64dev or f32dev) and collision kind (SRT, TRT or MRT); members
-    with a time-dependent force are stepped with their times (step(nsteps, t0, dt)).  The batch holds
-    its members' contexts without owning them: close the batch before any member."""
+    """Several DeviceLattices advanced together: member k takes nsteps[k] steps (lbm_batch_*).
+    Small members take all their steps of a call in one block-resident launch (a thread-block
+    cluster per member, its populations in shared memory); the others are issued as one CUDA graph
+    with one kernel per global step over every member still running.  `schedule` picks the small
+    members: "measured" (the table tune_batch.py measured on the GPU, batch_schedule.json), None
+    (every member on the graph path) or an explicit {velocity set: {"resident_max_nodes",
+    "nodes_per_block"}} mapping; the results are the same bits either way.  Members must share
+    storage (f64, df64dev or f32dev) and collision kind (SRT, TRT or MRT); members with a
+    time-dependent force are stepped with their times (step(nsteps, t0, dt)).  The batch holds its
+    members' contexts without owning them: close the batch before any member."""
 
-    def __init__(self, lattices):
+    def __init__(self, lattices, schedule="measured"):
         L = N.lib()
         self.lattices = list(lattices)
         if any(not getattr(lat, "h", None) for lat in self.lattices):
@@ -248,6 +253,7 @@ class DeviceBatch:
             raise N.LbmError(st, "lbm_batch_create: members must share storage and collision kind (SRT, TRT, MRT), "
                                  "use f64 / df64dev / f32dev, and each appear once")
         self.h = h
+        self.set_schedule(schedule)
         for lat in self.lattices:  # weak: the batch's references keep the members, not the other way
             if not hasattr(lat, "_batches"):
                 lat._batches = weakref.WeakSet()
@@ -285,6 +291,13 @@ class DeviceBatch:
     def set_stream(self, stream_handle):
         self._open()
         self._check(N.lib().lbm_batch_set_stream(self.h, stream_handle or None))
+
+    def set_schedule(self, schedule="measured"):
+        """lbm_batch_set_schedule: which members step block-resident (see the class docstring)."""
+        from .batch_schedule import schedule_for
+        self._open()
+        st = schedule_for(self.lattices[0].storage, schedule)
+        self._check(N.lib().lbm_batch_set_schedule(self.h, C.byref(st) if st is not None else None))
 
     def synchronize(self):
         self._open()

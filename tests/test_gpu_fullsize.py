@@ -1,7 +1,9 @@
 """The metric's full-size workloads at their full run lengths, checked through size-independent
 properties.  Both flows are x-invariant, so every column of the big lattice must equal the
 oracle's run of a 3-column lattice of the same height (≤ 1e-12 relative on every population),
-all columns must be bitwise equal, and the periodic / bounce-back step conserves mass.
+all columns must be bitwise equal, and the periodic / bounce-back step conserves mass up to the
+rounding of each step's collision (FP64: ~1e-16 of the mass per step, so the bound grows with the
+run length).
 
   - D2Q9 TRT (magic Λ = 1/4) Poiseuille channel 4096 x 4096, bounce-back North / South,
     constant lattice force 1e-6, τ_s drawn from U[0.55, 1.5] with the benchmark's seed, u = 0
@@ -14,6 +16,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+MASS_TOL_PER_STEP = 1e-15  # relative mass drift allowed per step: the rounding of the node sums
 SEED = 20240611  # the benchmark's seed for τ_s
 
 
@@ -82,7 +85,7 @@ def test_channel_4096_2000_steps_matches_oracle(lbm_gpu, O, storage):
     mass1 = m.lattice.conserved()[0]
     f = m.f_stream
     m.close()
-    assert abs(mass1 - mass0) / mass0 < 1e-13
+    assert abs(mass1 - mass0) / mass0 < steps * MASS_TOL_PER_STEP
     assert _columns_equal(f)
     ref = _oracle_channel(O, n, steps, tau_s)
     err = float(np.max(np.abs(f[:, :, 0] - ref[:, :, 0]) / np.abs(ref[:, :, 0])))
@@ -104,7 +107,7 @@ def test_mrt_d2q37_shear_wave_2048_500_steps_matches_oracle(lbm_gpu, O, storage)
     mass1 = m.lattice.conserved()[0]
     f = m.f_stream
     m.close()
-    assert abs(mass1 - mass0) / mass0 < 1e-13
+    assert abs(mass1 - mass0) / mass0 < steps * MASS_TOL_PER_STEP
     assert _columns_equal(f)
     ref = _oracle_shear_wave(O, n, steps, tau)
     err = float(np.max(np.abs(f[:, :, 0] - ref[:, :, 0]) / np.abs(ref[:, :, 0])))
