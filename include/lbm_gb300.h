@@ -266,7 +266,9 @@ int32_t lbm_batch_reduce_fields(lbm_batch* batch, int32_t kind, const uint8_t* s
  *                          in shared memory (0: never; such members use the graph path);
  *   nodes_per_block[q]     nodes per CTA: a resident member runs on a thread-block cluster of
  *                          ceil(n / nodes_per_block[q]) CTAs, rounded up to a power of two, at
- *                          most 8, the pull crossing CTAs through distributed shared memory.
+ *                          most 8, the pull crossing CTAs through distributed shared memory;
+ *   split[q]               warps sharing each node's collision: 1, 2 or 4 (SRT / TRT with FP64 or
+ *                          float-float storage from D2Q9 up; 0 and other cases mean 1).
  * A member whose share of both population buffers would not fit one CTA's shared memory takes the
  * graph path.  Results are the same bits on either path (same populations, same collision
  * arithmetic).  lbm_batch_set_schedule(batch, NULL) puts every member on the graph path, the
@@ -274,6 +276,7 @@ int32_t lbm_batch_reduce_fields(lbm_batch* batch, int32_t kind, const uint8_t* s
 typedef struct {
   int64_t resident_max_nodes[7];
   int32_t nodes_per_block[7];
+  int32_t split[7];
 } lbm_batch_schedule;
 int32_t lbm_batch_set_schedule(lbm_batch* batch, const lbm_batch_schedule* schedule);
 /* Members issue their own calls on the batch's stream until the batch is destroyed (no ordering

@@ -53,7 +53,7 @@ class LbmAnalytic(C.Structure):
 
 
 class LbmBatchSchedule(C.Structure):
-    _fields_ = [("resident_max_nodes", C.c_int64 * 7), ("nodes_per_block", C.c_int32 * 7)]
+    _fields_ = [("resident_max_nodes", C.c_int64 * 7), ("nodes_per_block", C.c_int32 * 7), ("split", C.c_int32 * 7)]
 
 
 _lock = threading.Lock()

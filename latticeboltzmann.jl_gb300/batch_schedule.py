@@ -5,8 +5,8 @@ it is small, the block-resident path (all of its steps of a call in one launch o
 cluster, lbm_resident.cuh).  Both give the same bits; the choice is speed only.  The choice is
 read from ``batch_schedule.json`` beside this file, a table measured on the GPU by
 ``tune_batch.py`` (per storage and velocity set: the largest member that is faster resident, and
-the nodes per CTA that were fastest there).  A velocity set missing from the table takes the
-graph path.
+the nodes per CTA and the split of each node's collision over warps that were fastest there).  A
+velocity set missing from the table takes the graph path.
 """
 from __future__ import annotations
 
@@ -32,12 +32,14 @@ def measured_table():
 
 
 def schedule_struct(rows):
-    """An LbmBatchSchedule from {velocity set: {"resident_max_nodes": n, "nodes_per_block": p}}."""
+    """An LbmBatchSchedule from {velocity set: {"resident_max_nodes": n, "nodes_per_block": p, "split": w}}
+    ("split", the warps sharing a node's collision, defaults to 1)."""
     s = N.LbmBatchSchedule()
     for q, name in enumerate(QUAD_NAMES):
         row = rows.get(name) or {}
         s.resident_max_nodes[q] = int(row.get("resident_max_nodes", 0))
         s.nodes_per_block[q] = int(row.get("nodes_per_block", 0))
+        s.split[q] = int(row.get("split", 1))
     return s
 
 

@@ -28,7 +28,7 @@ cudaError_t batch_reduce_launch(int storage, int qid, int K, const void* statics
                                 double* out, cudaStream_t s);
 size_t batch_static_size(int storage);
 cudaError_t resident_launch(int storage, int coll, int qid, const void* statics, const ResidentDyn* dyn, int nmem,
-                            int csize, int stride, int threads, cudaStream_t s);
+                            int csize, int stride, int threads, int parts, cudaStream_t s);
 struct AdjArgs;
 cudaError_t adj_launch(int op, int qid, int storage, int coll, const void* params, AdjArgs a, const void* src, int pull,
                        const void* lam_next, void* lam_out, double* slots, int nblocks, const double* u0,
@@ -1123,6 +1123,16 @@ int resident_cluster(const lbm_batch* b, const lbm_ctx* c) {
   return csize;
 }
 
+// Warps sharing each node's collision in a resident launch (lbm_resident.cuh builds splits for
+// SRT / TRT with FP64 or float-float storage from D2Q9 up).
+int resident_parts(const lbm_batch* b, const lbm_ctx* c) {
+  const int s = b->schedule.split[c->qid];
+  if ((s != 2 && s != 4) || (b->coll != LBM_SRT && b->coll != LBM_TRT) || c->Q < 9 ||
+      (b->storage != LBM_STORE_F64 && b->storage != LBM_STORE_DF64_DEV))
+    return 1;
+  return s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1251,7 +1261,7 @@ int32_t lbm_batch_set_schedule(lbm_batch* b, const lbm_batch_schedule* schedule)
     return LBM_OK;
   }
   for (int q = 0; q < 7; ++q)
-    if (schedule->resident_max_nodes[q] < 0 || schedule->nodes_per_block[q] < 0)
+    if (schedule->resident_max_nodes[q] < 0 || schedule->nodes_per_block[q] < 0 || schedule->split[q] < 0)
       return bfail(b, LBM_ERR_INVALID, "schedule: negative limit");
   b->schedule = *schedule;
   return LBM_OK;
@@ -1285,7 +1295,7 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
   for (int k = 0; k < count; ++k)
     if (nsteps[k] > 0 && (csize[k] = resident_cluster(b, b->members[k])) > 0) gsteps[k] = 0;
   struct ResidentGroup {
-    int qid, csize, first, nmem, stride;
+    int qid, csize, parts, first, nmem, stride;
   };
   std::vector<ResidentDyn> rdyn;
   std::vector<ResidentGroup> rgroups;
@@ -1301,7 +1311,7 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
       const int k = res[r];
       const lbm_ctx* c = b->members[k];
       if (rgroups.empty() || rgroups.back().qid != c->qid || rgroups.back().csize != csize[k])
-        rgroups.push_back({c->qid, csize[k], (int)r, 0, 0});
+        rgroups.push_back({c->qid, csize[k], resident_parts(b, c), (int)r, 0, 0});
       ResidentGroup& g = rgroups.back();
       ResidentDyn d{};
       d.member = k;
@@ -1369,11 +1379,13 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
     for (size_t gi = 0; gi < rgroups.size(); ++gi) {
       const ResidentGroup& g = rgroups[gi];
       cudaStream_t st = b->res_streams[gi];
-      const int threads = std::min(kResidentThreads, (g.stride + 31) / 32 * 32);
+      // node groups of 32 (one node per lane), each on `parts` warps, at most kResidentThreads threads
+      const int groups = std::max(1, std::min((g.stride + 31) / 32, kResidentThreads / (32 * g.parts)));
+      const int threads = groups * 32 * g.parts;
       cudaError_t e = cudaStreamWaitEvent(st, b->res_fork, 0);
       if (e == cudaSuccess)
         e = resident_launch(b->storage, b->coll, g.qid, b->d_static, b->d_rdyn + g.first, g.nmem, g.csize, g.stride,
-                            threads, st);
+                            threads, g.parts, st);
       if (e == cudaSuccess) e = cudaEventRecord(b->res_events[gi], st);
       if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(e));
     }

@@ -20,13 +20,15 @@
 // collision arithmetic are the graph path's, so a member gives the same bits either way.
 #pragma once
 
+#include <atomic>
+
 #include <cooperative_groups.h>
 
 #include "lbm_batch.cuh"
 
 namespace lbm {
 
-constexpr int kResidentThreads = 128;   // threads per CTA (at most)
+constexpr int kResidentThreads = 256;   // threads per CTA (at most)
 constexpr int kResidentMaxCluster = 8;  // CTAs per member (portable cluster size)
 constexpr size_t kResidentMaxSmem = 227 * 1024;
 
@@ -119,7 +121,13 @@ __device__ __forceinline__ void resident_pull(const StepParams<CT>& p, const Clu
 // member blockIdx.x / C, cluster rank blockIdx.x % C.  Dynamic shared memory: two buffers of Q
 // planes of `stride` populations.  Every CTA runs every step and every cluster barrier, including
 // CTAs that own no node (members smaller than C), so the barriers always complete.
-template <class L, class S, int COLL>
+//
+// PARTS > 1 splits each node's SRT / TRT collision over PARTS warps (owns_pop, lbm_step.cuh):
+// warp w takes the nodes of group w / PARTS (32 nodes, one per lane) and computes the outputs of
+// part w % PARTS, which is the same for the whole warp, so the split costs no divergence.  A
+// small member is bound by the latency of one warp's collision (FP64 issues at two lanes per SM
+// per clock), and a split shortens that chain to the node-wide sums plus a share of the outputs.
+template <class L, class S, int COLL, int PARTS>
 __global__ void __launch_bounds__(kResidentThreads) resident_step_kernel(
     const BatchStatic<typename S::C>* __restrict__ statics, const ResidentDyn* __restrict__ dyn, int csize,
     int stride) {
@@ -133,7 +141,8 @@ __global__ void __launch_bounds__(kResidentThreads) resident_step_kernel(
   const ResidentDyn d = dyn[blockIdx.x / csize];
   const BatchStatic<CT>& m = statics[d.member];
   const StepParams<CT>& p = m.p;
-  T* buf[2] = {reinterpret_cast<T*>(resident_smem), reinterpret_cast<T*>(resident_smem) + (size_t)L::Q * stride};
+  T* cur = reinterpret_cast<T*>(resident_smem);      // the state
+  T* nxt = cur + (size_t)L::Q * stride;                // the next step's state
   const int n = (int)p.n;
   const int base = rank * d.chunk;
   const int count = max(0, min(n - base, d.chunk));
@@ -142,38 +151,49 @@ __global__ void __launch_bounds__(kResidentThreads) resident_step_kernel(
   const T* g = static_cast<const T*>(d.cur0 ? m.buf1 : m.buf0);
   for (int k = threadIdx.x; k < L::Q * count; k += blockDim.x) {
     const int i = k / count, j = k - i * count;
-    buf[0][(size_t)i * stride + j] = g[(size_t)i * n + base + j];
+    cur[(size_t)i * stride + j] = g[(size_t)i * n + base + j];
   }
   cluster.sync();
 
-  int a = 0;
+  const int warp = threadIdx.x >> 5;
+  const int part = warp % PARTS;                      // the same for every lane of a warp
+  const int first = (warp / PARTS) * 32 + (threadIdx.x & 31);
+  const int jstep = (blockDim.x / (32 * PARTS)) * 32;  // nodes covered by all groups of the CTA
   for (long long t = 0; t < d.steps; ++t) {
-    const ClusterPlanes<T> src{buf[a], rank, d.chunk, stride};
-    T* dst = buf[a ^ 1];
-    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+    const ClusterPlanes<T> src{cur, rank, d.chunk, stride};
+    T* dst = nxt;
+    for (int j = first; j < count; j += jstep) {
       const int node = base + j;
       const int y = node / p.nx;
       const int x = node - y * p.nx;
       CT v[L::Q];
       if (t == 0 && d.phase0 == 0) {
 #pragma unroll
-        for (int i = 0; i < L::Q; ++i) v[i] = V::ld(buf[a] + (size_t)i * stride + j);
+        for (int i = 0; i < L::Q; ++i) v[i] = V::ld(cur + (size_t)i * stride + j);
       } else {
         resident_pull<L, V>(p, src, x, y, j, v);
       }
-      collide_node<L, S, COLL>(p, x, y, v, [&] { return (double)(d.t0 + t) * d.dt; });
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) V::st(dst + (size_t)i * stride + j, v[i]);
+      static_for<0, PARTS>([&](auto P) {
+        constexpr int PP = decltype(P)::value;
+        if (part == PP) {
+          collide_node<L, S, COLL, PARTS, PP>(p, x, y, v, [&] { return (double)(d.t0 + t) * d.dt; });
+          static_for<0, L::Q>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            if constexpr (owns_pop<L, PARTS, PP>(i)) V::st(dst + (size_t)i * stride + j, v[i]);
+          });
+        }
+      });
     }
     cluster.sync();  // this step's writes visible, and every read of the old buffer done
-    a ^= 1;
+    nxt = cur;
+    cur = dst;
   }
 
   // the final state into the buffer the member's parity names after d.steps steps
   T* out = static_cast<T*>(((d.cur0 + d.steps) & 1) ? m.buf1 : m.buf0);
   for (int k = threadIdx.x; k < L::Q * count; k += blockDim.x) {
     const int i = k / count, j = k - i * count;
-    out[(size_t)i * n + base + j] = buf[a][(size_t)i * stride + j];
+    out[(size_t)i * n + base + j] = cur[(size_t)i * stride + j];
   }
 }
 
@@ -183,12 +203,28 @@ constexpr size_t resident_smem_bytes(int stride) {
   return 2 * (size_t)L::Q * (size_t)stride * sizeof(typename S::T);
 }
 
-template <class L, class S, int COLL>
+// The kernel may use up to kResidentMaxSmem of dynamic shared memory: set once per device (an
+// attribute change while the same kernel runs on another stream would order the launches).
+template <class K>
+cudaError_t allow_resident_smem(K kernel) {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load() & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResidentMaxSmem);
+  if (e == cudaSuccess) done.fetch_or(bit);
+  return e;
+}
+
+template <class L, class S, int COLL, int PARTS>
 cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
                               int threads, cudaStream_t s) {
-  auto kernel = resident_step_kernel<L, S, COLL>;
+  auto kernel = resident_step_kernel<L, S, COLL, PARTS>;
   const size_t smem = resident_smem_bytes<L, S>(stride);
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (threads % (32 * PARTS) != 0) return cudaErrorInvalidValue;
+  cudaError_t e = allow_resident_smem(kernel);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nmem * csize));
@@ -207,34 +243,53 @@ cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int n
   return cudaGetLastError();
 }
 
+// Splits are built for the pair-form collisions (SRT, TRT) of the FP64-class storages from D2Q9
+// up, where one warp's collision chain is long; elsewhere a node's collision stays in one warp.
+template <class L, class S>
+constexpr bool resident_splits() {
+  return (S::id == LBM_STORE_F64 || S::id == LBM_STORE_DF64_DEV) && L::Q >= 9;
+}
+
+template <class L, class S, int COLL>
+cudaError_t resident_launch_c(const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
+                              int threads, int parts, cudaStream_t s) {
+  if constexpr ((COLL == LBM_SRT || COLL == LBM_TRT) && resident_splits<L, S>()) {
+    if (parts == 2) return resident_launch_k<L, S, COLL, 2>(statics, dyn, nmem, csize, stride, threads, s);
+    if (parts == 4) return resident_launch_k<L, S, COLL, 4>(statics, dyn, nmem, csize, stride, threads, s);
+  }
+  if (parts != 1) return cudaErrorInvalidValue;
+  return resident_launch_k<L, S, COLL, 1>(statics, dyn, nmem, csize, stride, threads, s);
+}
+
 template <class L, class S>
 cudaError_t resident_launch_s(int coll, const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
-                              int threads, cudaStream_t s) {
+                              int threads, int parts, cudaStream_t s) {
   switch (coll) {
-    case LBM_SRT: return resident_launch_k<L, S, LBM_SRT>(statics, dyn, nmem, csize, stride, threads, s);
-    case LBM_TRT: return resident_launch_k<L, S, LBM_TRT>(statics, dyn, nmem, csize, stride, threads, s);
-    case LBM_MRT: return resident_launch_k<L, S, LBM_MRT>(statics, dyn, nmem, csize, stride, threads, s);
+    case LBM_SRT: return resident_launch_c<L, S, LBM_SRT>(statics, dyn, nmem, csize, stride, threads, parts, s);
+    case LBM_TRT: return resident_launch_c<L, S, LBM_TRT>(statics, dyn, nmem, csize, stride, threads, parts, s);
+    case LBM_MRT: return resident_launch_c<L, S, LBM_MRT>(statics, dyn, nmem, csize, stride, threads, parts, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
 // One resident launch: `nmem` members of velocity set L, each on a cluster of `csize` CTAs of
-// `threads` threads with `stride` nodes per plane in shared memory.
+// `threads` threads (a multiple of 32 * parts) with `stride` nodes per plane in shared memory, each
+// node's collision split over `parts` warps (1, 2 or 4).
 template <class L>
 cudaError_t resident_launch_set(int storage, int coll, const void* statics, const ResidentDyn* dyn, int nmem,
-                                int csize, int stride, int threads, cudaStream_t s) {
+                                int csize, int stride, int threads, int parts, cudaStream_t s) {
   if (nmem <= 0) return cudaSuccess;
   if (csize < 1 || csize > kResidentMaxCluster || threads < 32 || threads > kResidentThreads) return cudaErrorInvalidValue;
   switch (storage) {
     case LBM_STORE_F64:
       if (resident_smem_bytes<L, F64>(stride) > kResidentMaxSmem) return cudaErrorInvalidValue;
-      return resident_launch_s<L, F64>(coll, statics, dyn, nmem, csize, stride, threads, s);
+      return resident_launch_s<L, F64>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
     case LBM_STORE_DF64_DEV:
       if (resident_smem_bytes<L, DF64Dev>(stride) > kResidentMaxSmem) return cudaErrorInvalidValue;
-      return resident_launch_s<L, DF64Dev>(coll, statics, dyn, nmem, csize, stride, threads, s);
+      return resident_launch_s<L, DF64Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
     case LBM_STORE_F32_DEV:
       if (resident_smem_bytes<L, F32Dev>(stride) > kResidentMaxSmem) return cudaErrorInvalidValue;
-      return resident_launch_s<L, F32Dev>(coll, statics, dyn, nmem, csize, stride, threads, s);
+      return resident_launch_s<L, F32Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -244,7 +299,7 @@ cudaError_t resident_launch_set(int storage, int coll, const void* statics, cons
 #define LBM_RESIDENT_INSTANTIATE(NAME, LAT)                                                                    \
   namespace lbm {                                                                                              \
   cudaError_t resident_launch_##NAME(int storage, int coll, const void* statics, const ResidentDyn* dyn,       \
-                                     int nmem, int csize, int stride, int threads, cudaStream_t s) {           \
-    return resident_launch_set<LAT>(storage, coll, statics, dyn, nmem, csize, stride, threads, s);             \
+                                     int nmem, int csize, int stride, int threads, int parts, cudaStream_t s) { \
+    return resident_launch_set<LAT>(storage, coll, statics, dyn, nmem, csize, stride, threads, parts, s);      \
   }                                                                                                            \
   }

@@ -474,6 +474,32 @@ __host__ __device__ constexpr bool class_first(int i) {
   return true;
 }
 
+// A node's collision split over PARTS warps (the block-resident batched kernel, lbm_resident.cuh):
+// every part computes the node-wide quantities, and part PART computes and owns the outputs of the
+// opposite pairs whose ordinal (pairs counted in population order) is PART modulo PARTS, the rest
+// population going to part 0.  Each output is formed by the same operations whichever part forms
+// it, so a split collision gives the bits of the whole one.
+template <class L>
+__host__ __device__ constexpr int pair_ordinal(int i) {  // i: the lower index of an opposite pair
+  int k = 0;
+  for (int j = 0; j < i; ++j)
+    if (L::opp(j) > j) ++k;
+  return k;
+}
+template <class L, int PARTS, int PART>
+__host__ __device__ constexpr bool owns_pop(int i) {
+  if (PARTS == 1) return true;
+  const int o = L::opp(i);
+  if (o == i) return PART == 0;
+  return pair_ordinal<L>(o < i ? o : i) % PARTS == PART;
+}
+template <class L, int PARTS, int PART>
+__host__ __device__ constexpr bool class_needed(int cls) {  // a population of class cls is PART's output
+  for (int j = 0; j < L::Q; ++j)
+    if (vclass<L>(j) == cls && owns_pop<L, PARTS, PART>(j)) return true;
+  return false;
+}
+
 // SRT / TRT in "pair form" (all storages).  Opposite populations enter only through their
 // sum s and difference d, which give both the moments (δρ = Σ s, j = Σ c d) and the TRT
 // symmetric / antisymmetric parts; the equilibrium is built from j' = ρ(u + τF) directly, with
@@ -489,7 +515,7 @@ __host__ __device__ constexpr bool class_first(int i) {
 // FP32 keeps ω_a (w1 X) with the FP32-exact w1, so the equilibrium's momentum stays exact.
 // CT is the type of the node values and PT that of the parameters: the same type, or packed FP32
 // pairs (pf2, two nodes) with FP32 parameters.
-template <class L, bool DEV, class CT, class PT>
+template <class L, bool DEV, int PARTS = 1, int PART = 0, class CT, class PT>
 __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT sFx, CT sFy, bool has_force) {
   constexpr bool F32 = std::is_same<CT, float>::value || std::is_same<CT, pf2>::value;
   CT sp[L::Q], dp[L::Q];
@@ -541,7 +567,7 @@ __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT
   CT b0[16], b2[16], b4[16], a3[16];
   static_for<0, L::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    if constexpr (class_first<L>(i)) {
+    if constexpr (class_first<L>(i) && class_needed<L, PARTS, PART>(vclass<L>(i))) {
       constexpr int k = vclass<L>(i);
       b0[k] = p.pws[i] * D0;
       if constexpr (L::EQ >= 2) b2[k] = p.pws[i] * D2;
@@ -551,9 +577,9 @@ __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT
   });
   static_for<0, L::Q>([&](auto I) {
     constexpr int i = decltype(I)::value, o = L::opp(i), k = vclass<L>(i);
-    if constexpr (o == i) {
+    if constexpr (o == i && PART == 0) {
       v[i] = prod_add_out(p.pa_s2, v[i], b0[k]);
-    } else if constexpr (o > i) {
+    } else if constexpr (o > i && owns_pop<L, PARTS, PART>(i)) {
       CT X;
       bool xs = false;
       acc_add<L::cx(i)>(X, xs, jx);
@@ -585,8 +611,11 @@ __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT
 //   MRT  mrt.jl:56-118   regularised projection (mrt_collide)
 //   ITER iterative_initialization.jl:41-60   feq = w ρ + nonlinear term
 // `time()` gives the physical time of the step (step_time(p), or a batch member's own).
-template <class L, class S, int COLL, class CT, class TimeFn>
+// PARTS / PART split an SRT / TRT collision over warps (see owns_pop); MRT and the iterative
+// collision are never split.
+template <class L, class S, int COLL, int PARTS = 1, int PART = 0, class CT, class TimeFn>
 __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int y, CT* v, TimeFn&& time) {
+  static_assert(PARTS == 1 || COLL == LBM_SRT || COLL == LBM_TRT, "only the pair-form collisions split");
   constexpr bool DEV = S::DEV;
   if constexpr (COLL == LBM_ITERATIVE_INIT) {
     CT s = v[0];
@@ -605,7 +634,7 @@ __device__ __forceinline__ void collide_node(const StepParams<CT>& p, int x, int
     const bool has_force = p.force_kind != LBM_FORCE_NONE;
     if (has_force) node_shifted_force(p, x, y, sFx, sFy, time);
     if constexpr (COLL == LBM_MRT) mrt_collide<L, DEV>(p, v, sFx, sFy, has_force);
-    else collide_pairs<L, DEV>(p, v, sFx, sFy, has_force);
+    else collide_pairs<L, DEV, PARTS, PART>(p, v, sFx, sFy, has_force);
   }
 }
 

@@ -5,10 +5,12 @@ For every storage (f64, df64dev, f32dev) and velocity set, batches of M identica
 lattices with a constant force are stepped K steps (the second call of each configuration is
 timed with CUDA events, so graph capture is not counted), for member sizes from 24 to 4096 nodes:
   - on the graph path (schedule None), and
-  - block-resident with 16, 32, 64 and 128 nodes per CTA.
-A velocity set's row is the largest member size at which the best resident configuration beats
-the graph path (every smaller measured size beating it too), with the nodes per CTA that was
-fastest there.  Both paths give the same bits, so the table changes speed only.
+  - block-resident with 16, 32 and 64 nodes per CTA, each node's collision on 1, 2 or 4 warps
+    (splits exist for SRT / TRT with FP64 or float-float storage from D2Q9 up).
+A velocity set's row is the largest member size up to which the best resident configuration beats
+the graph path at every measured size, with the configuration whose time relative to the graph
+path, summed over those sizes, is least.  Both paths give the same bits, so the table changes
+speed only.
 
   python -m latticeboltzmann_gb300.tune_batch   (or: python latticeboltzmann.jl_gb300/tune_batch.py)
 """
@@ -22,7 +24,8 @@ import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SHAPES = ((8, 3), (16, 3), (32, 3), (64, 3), (16, 16), (32, 32), (64, 64))
-PER_BLOCK = (16, 32, 64, 128)
+PER_BLOCK = (16, 32, 64)
+SPLITS = (1, 2, 4)
 STORAGES = ("f64", "df64dev", "f32dev")
 ELEM = {"f64": 8, "df64dev": 8, "f32dev": 4}
 
@@ -96,23 +99,31 @@ def tune(members=16, steps=200, storages=STORAGES, quads=None, log=sys.stderr):
                     lats.append(lat)
                 f0 = [lat.download() for lat in lats]
                 res = {"graph": time_batch(torch, lbm, lats, f0, steps, None) / steps * 1e6}
+                splits = SPLITS if storage in ("f64", "df64dev") and q.Q >= 9 else (1,)
                 for per in PER_BLOCK:
-                    if resident_fits(q.Q, n, per, ELEM[storage]):
-                        sched = {qn: {"resident_max_nodes": n, "nodes_per_block": per}}
-                        res[f"resident{per}"] = time_batch(torch, lbm, lats, f0, steps, sched) / steps * 1e6
+                    if not resident_fits(q.Q, n, per, ELEM[storage]):
+                        continue
+                    for split in splits:
+                        sched = {qn: {"resident_max_nodes": n, "nodes_per_block": per, "split": split}}
+                        res[f"{per}x{split}"] = time_batch(torch, lbm, lats, f0, steps, sched) / steps * 1e6
                 for lat in lats:
                     lat.close()
                 per_q[str(n)] = {k: round(v, 3) for k, v in res.items()}
-                rbest = min(((v, k) for k, v in res.items() if k != "graph"), default=(float("inf"), None))
-                best_rows.append((n, res["graph"], rbest))
+                best_rows.append((n, res))
                 print(f"{storage} {qn} n={n}: " + ", ".join(f"{k} {v:.2f}" for k, v in res.items()) + " us/step",
                       file=log, flush=True)
-            # the largest size below which resident always wins, and its best nodes per CTA
-            row = {"resident_max_nodes": 0, "nodes_per_block": 0}
-            for n, g, (rv, rk) in best_rows:
-                if rk is None or rv >= g:
+            # the sizes up to the first one where no resident configuration beats the graph path
+            wins = []
+            for n, res in best_rows:
+                if min((v for k, v in res.items() if k != "graph"), default=float("inf")) >= res["graph"]:
                     break
-                row = {"resident_max_nodes": n, "nodes_per_block": int(rk[len("resident"):])}
+                wins.append((n, res))
+            row = {"resident_max_nodes": 0, "nodes_per_block": 0, "split": 1}
+            if wins:
+                keys = [k for k in wins[-1][1] if k != "graph" and all(k in r for _, r in wins)]
+                best = min(keys, key=lambda k: sum(r[k] / r["graph"] for _, r in wins))
+                per, split = (int(v) for v in best.split("x"))
+                row = {"resident_max_nodes": wins[-1][0], "nodes_per_block": per, "split": split}
             rows[qn] = row
             meas[qn] = per_q
         table["storages"][storage] = rows

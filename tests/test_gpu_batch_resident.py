@@ -50,8 +50,8 @@ def _models(lbm, storage, coll, specs=SPECS):
     return out
 
 
-def _resident(per, max_nodes=10 ** 9):
-    return {q: {"resident_max_nodes": max_nodes, "nodes_per_block": per} for q in QUADS}
+def _resident(per, max_nodes=10 ** 9, split=1):
+    return {q: {"resident_max_nodes": max_nodes, "nodes_per_block": per, "split": split} for q in QUADS}
 
 
 def _run(lbm, storage, coll, schedule, specs=SPECS, calls=2):
@@ -78,11 +78,14 @@ def _same(fa, fb, coll, storage):
 
 @pytest.mark.parametrize("storage", ["f64", "df64dev", "f32dev"])
 @pytest.mark.parametrize("coll", ["SRT", "TRT", "MRT"])
-@pytest.mark.parametrize("per", [8, 32, 128])
-def test_resident_equals_graph_path(lbm_gpu, storage, coll, per):
+@pytest.mark.parametrize("per", [8, 128])
+@pytest.mark.parametrize("split", [1, 2, 4])
+def test_resident_equals_graph_path(lbm_gpu, storage, coll, per, split):
+    """split > 1 spreads each node's SRT / TRT collision over 2 or 4 warps where the library builds
+    splits (FP64 and float-float from D2Q9 up); the other cases run unsplit."""
     lbm = lbm_gpu
     ref, graph_launches = _run(lbm, storage, coll, None)
-    got, launches = _run(lbm, storage, coll, _resident(per))
+    got, launches = _run(lbm, storage, coll, _resident(per, split=split))
     _same(got, ref, coll, storage)
     # graph: one kernel per global step of each velocity set's longest member; resident: one launch
     # per (velocity set, cluster size)
@@ -126,8 +129,8 @@ def _shear_model(lbm, qname, nx, ny, storage, seed):
 
 
 @pytest.mark.parametrize("storage", ["f64", "df64dev", "f32dev"])
-@pytest.mark.parametrize("per", [4, 64])
-def test_resident_time_dependent_force(lbm_gpu, storage, per):
+@pytest.mark.parametrize("per,split", [(4, 1), (64, 1), (8, 4), (64, 2)])
+def test_resident_time_dependent_force(lbm_gpu, storage, per, split):
     """Members with the time-dependent shear force, stepped with their own times: resident equals
     each lattice stepped alone through lbm_step (bitwise)."""
     lbm = lbm_gpu
@@ -136,7 +139,7 @@ def test_resident_time_dependent_force(lbm_gpu, storage, per):
     steps = np.array([s[3] for s in SHEAR])
     t0 = np.array([s[4] for s in SHEAR])
     dt = np.array([s[5] for s in SHEAR])
-    batch = lbm.DeviceBatch([m.lattice for m in members], schedule=_resident(per))
+    batch = lbm.DeviceBatch([m.lattice for m in members], schedule=_resident(per, split=split))
     batch.step(steps, t0, dt)
     batch.step(steps, t0 + steps, dt)
     batch.close()
