@@ -30,7 +30,9 @@ namespace lbm {
 
 constexpr int kResidentThreads = 256;   // threads per CTA (at most)
 constexpr int kResidentMaxCluster = 8;  // CTAs per member (portable cluster size)
-constexpr size_t kResidentMaxSmem = 227 * 1024;
+// Shared memory a resident member's CTA may plan on: 200 KB, below the opt-in limit per block
+// (227 KB on this GPU) with room for the kernel's own static shared memory.
+constexpr size_t kResidentMaxSmem = 200 * 1024;
 
 // One member of a resident launch.
 struct ResidentDyn {
@@ -203,19 +205,33 @@ constexpr size_t resident_smem_bytes(int stride) {
   return 2 * (size_t)L::Q * (size_t)stride * sizeof(typename S::T);
 }
 
-// The kernel may use up to kResidentMaxSmem of dynamic shared memory: set once per device (an
-// attribute change while the same kernel runs on another stream would order the launches).
+// The largest dynamic shared memory a CTA of `kernel` may use on the current device: the device's
+// opt-in limit per block less the kernel's static shared memory.  The kernel's attribute is raised
+// to that once per device (an attribute change while the same kernel runs on another stream could
+// order the launches), and the result is kept.
 template <class K>
-cudaError_t allow_resident_smem(K kernel) {
-  static std::atomic<unsigned long long> done{0};
+cudaError_t allow_resident_smem(K kernel, size_t* limit) {
+  static std::atomic<long long> allowed[64];  // per device: 0 unknown, else the limit + 1
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  const unsigned long long bit = 1ull << (dev & 63);
-  if (done.load() & bit) return cudaSuccess;
-  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResidentMaxSmem);
-  if (e == cudaSuccess) done.fetch_or(bit);
-  return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  long long have = allowed[dev].load();
+  if (have == 0) {
+    int optin = 0;
+    cudaFuncAttributes fa{};
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    const long long lim = (long long)optin - (long long)fa.sharedSizeBytes;
+    if (lim <= 0) return cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim);
+    if (e != cudaSuccess) return e;
+    have = lim + 1;
+    allowed[dev].store(have);
+  }
+  *limit = (size_t)(have - 1);
+  return cudaSuccess;
 }
 
 template <class L, class S, int COLL, int PARTS>
@@ -224,8 +240,10 @@ cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int n
   auto kernel = resident_step_kernel<L, S, COLL, PARTS>;
   const size_t smem = resident_smem_bytes<L, S>(stride);
   if (threads % (32 * PARTS) != 0) return cudaErrorInvalidValue;
-  cudaError_t e = allow_resident_smem(kernel);
+  size_t limit = 0;
+  cudaError_t e = allow_resident_smem(kernel, &limit);
   if (e != cudaSuccess) return e;
+  if (smem > limit) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nmem * csize));
   cfg.blockDim = dim3((unsigned)threads);
@@ -282,13 +300,10 @@ cudaError_t resident_launch_set(int storage, int coll, const void* statics, cons
   if (csize < 1 || csize > kResidentMaxCluster || threads < 32 || threads > kResidentThreads) return cudaErrorInvalidValue;
   switch (storage) {
     case LBM_STORE_F64:
-      if (resident_smem_bytes<L, F64>(stride) > kResidentMaxSmem) return cudaErrorInvalidValue;
       return resident_launch_s<L, F64>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
     case LBM_STORE_DF64_DEV:
-      if (resident_smem_bytes<L, DF64Dev>(stride) > kResidentMaxSmem) return cudaErrorInvalidValue;
       return resident_launch_s<L, DF64Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
     case LBM_STORE_F32_DEV:
-      if (resident_smem_bytes<L, F32Dev>(stride) > kResidentMaxSmem) return cudaErrorInvalidValue;
       return resident_launch_s<L, F32Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
     default: return cudaErrorInvalidValue;
   }

@@ -47,12 +47,12 @@ def _package():
 
 def resident_fits(Q, n, per, elem):
     """The library's rule (resident_cluster in lbm_api.cu): cluster of ceil(n / per) CTAs rounded up
-    to a power of two, at most 8, and both buffers of a CTA's share within 227 KB."""
+    to a power of two, at most 8, and both buffers of a CTA's share within 200 KB."""
     c = 1
     while c < 8 and c * per < n:
         c *= 2
     chunk = -(-n // c)
-    return 2 * Q * chunk * elem <= 227 * 1024
+    return 2 * Q * chunk * elem <= 200 * 1024
 
 
 def time_batch(torch, lbm, lats, f0, steps, schedule):
