@@ -1387,7 +1387,12 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
         e = resident_launch(b->storage, b->coll, g.qid, b->d_static, b->d_rdyn + g.first, g.nmem, g.csize, g.stride,
                             threads, g.parts, st);
       if (e == cudaSuccess) e = cudaEventRecord(b->res_events[gi], st);
-      if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(e));
+      if (e != cudaSuccess) {
+        char what[200];
+        std::snprintf(what, sizeof what, "resident launch (velocity set %d, %d members, clusters of %d CTAs x %d threads, "
+                      "%d nodes per plane, %d warps per node): ", g.qid, g.nmem, g.csize, threads, g.stride, g.parts);
+        return bfail(b, LBM_ERR_CUDA, std::string(what) + cudaGetErrorString(e));
+      }
     }
   }
   b->res_launches = (int64_t)rgroups.size();
