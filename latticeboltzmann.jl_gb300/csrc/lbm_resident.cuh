@@ -208,10 +208,10 @@ constexpr size_t resident_smem_bytes(int stride) {
 // The largest dynamic shared memory a CTA of `kernel` may use on the current device: the device's
 // opt-in limit per block less the kernel's static shared memory.  The kernel's attribute is raised
 // to that once per device (an attribute change while the same kernel runs on another stream could
-// order the launches), and the result is kept.
+// order the launches), and the result is kept in `allowed` (per device: 0 unknown, else the limit
+// + 1), which the caller keeps for this one kernel.
 template <class K>
-cudaError_t allow_resident_smem(K kernel, size_t* limit) {
-  static std::atomic<long long> allowed[64];  // per device: 0 unknown, else the limit + 1
+cudaError_t allow_resident_smem(K kernel, std::atomic<long long>* allowed, size_t* limit) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -238,10 +238,11 @@ template <class L, class S, int COLL, int PARTS>
 cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
                               int threads, cudaStream_t s) {
   auto kernel = resident_step_kernel<L, S, COLL, PARTS>;
+  static std::atomic<long long> allowed[64];  // this kernel's shared-memory limit per device
   const size_t smem = resident_smem_bytes<L, S>(stride);
   if (threads % (32 * PARTS) != 0) return cudaErrorInvalidValue;
   size_t limit = 0;
-  cudaError_t e = allow_resident_smem(kernel, &limit);
+  cudaError_t e = allow_resident_smem(kernel, allowed, &limit);
   if (e != cudaSuccess) return e;
   if (smem > limit) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
