@@ -59,9 +59,11 @@ __device__ __forceinline__ dd ladd(dd a, dd b) { return add_lazy(a, b); }
 __device__ __forceinline__ dd lsub(dd a, dd b) { return add_lazy(a, -b); }
 #endif
 
-// Multiply-add shapes c + a b, c - a b, a b + c, a b - c of the collision.  FP32 / FP64: the
-// plain expressions, which the compiler contracts into FMAs; float-float: lazy sums of products;
-// packed FP32 pairs (lbm_pf2.cuh): one packed FMA.
+// Multiply-add shapes c + a b, c - a b, a b + c, a b - c of the collision.  FP32 / FP64: explicit
+// FMAs (below), so that which product is fused never depends on how often the compiler sees it
+// used -- the same collision code then rounds alike whether it is inlined whole or split over
+// warps (lbm_resident.cuh); float-float: lazy sums of products; packed FP32 pairs (lbm_pf2.cuh):
+// one packed FMA.
 template <class CT>
 __device__ __forceinline__ CT add_prod(CT c, CT a, CT b) { return ladd(c, a * b); }
 template <class CT>
@@ -78,6 +80,12 @@ __device__ __forceinline__ CT prod_add_out(CT a, CT b, CT c) { return a * b + c;
 __device__ __forceinline__ float add_prod(float c, float a, float b) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float sub_prod(float c, float a, float b) { return __fmaf_rn(-a, b, c); }
 __device__ __forceinline__ float prod_add(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// FP64: explicit FMAs as well
+__device__ __forceinline__ double add_prod(double c, double a, double b) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ double sub_prod(double c, double a, double b) { return __fma_rn(-a, b, c); }
+__device__ __forceinline__ double prod_add(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ double prod_sub(double a, double b, double c) { return __fma_rn(a, b, -c); }
+__device__ __forceinline__ double prod_add_out(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float prod_sub(float a, float b, float c) { return __fmaf_rn(a, b, -c); }
 __device__ __forceinline__ float prod_add_out(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 #endif
