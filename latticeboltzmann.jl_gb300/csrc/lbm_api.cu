@@ -28,7 +28,7 @@ cudaError_t batch_reduce_launch(int storage, int qid, int K, const void* statics
                                 double* out, cudaStream_t s);
 size_t batch_static_size(int storage);
 cudaError_t resident_launch(int storage, int coll, int qid, const void* statics, const ResidentDyn* dyn, int nmem,
-                            int csize, int stride, int threads, int parts, cudaStream_t s);
+                            int csize, int stride, int threads, int parts, size_t smem_min, cudaStream_t s);
 struct AdjArgs;
 cudaError_t adj_launch(int op, int qid, int storage, int coll, const void* params, AdjArgs a, const void* src, int pull,
                        const void* lam_next, void* lam_out, double* slots, int nblocks, const double* u0,
@@ -1023,6 +1023,8 @@ struct lbm_batch {
   std::vector<cudaEvent_t> res_events;
   cudaEvent_t res_fork = nullptr;
   int64_t res_launches = 0;
+  int sm_count = 0;                // the device's SMs and shared memory per SM (bytes)
+  int smem_per_sm = 0;
   ReduceArgs* d_rargs = nullptr;  // per member, set up by the first reduction
   std::vector<ReduceArgs> h_rargs; // host copy of the same
   ReduceArgs* d_rargs_call = nullptr;  // per member, with this call's analytic fields
@@ -1168,6 +1170,11 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
     if (b->storage == LBM_STORE_F64) fill_static(*reinterpret_cast<BatchStatic<double>*>(slot), c->pd, c);
     else if (b->storage == LBM_STORE_DF64_DEV) fill_static(*reinterpret_cast<BatchStatic<dd>*>(slot), c->px, c);
     else fill_static(*reinterpret_cast<BatchStatic<float>*>(slot), c->pf, c);
+  }
+  if (cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&b->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, b->device) != cudaSuccess) {
+    drop_reported_error();
+    b->sm_count = b->smem_per_sm = 0;
   }
   if (!make_stream(&b->own_stream) || !make_event(&b->done) || !make_event(&b->staged) ||
       !dev_malloc(&b->d_static, sb * count) ||
@@ -1376,6 +1383,12 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
       b->res_events.push_back(ev);
     }
     if (cudaEventRecord(b->res_fork, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "resident fork");
+    // When every CTA of the call can have an SM of its own, each asks for more than half an SM's
+    // shared memory, so that no two share an SM's FP64 units: a small member's step is bound by
+    // the latency of its warps' collision chains, which a second CTA on the SM would lengthen.
+    long long ctas = 0;
+    for (const ResidentGroup& g : rgroups) ctas += (long long)g.nmem * g.csize;
+    const size_t smem_min = (b->sm_count > 0 && ctas <= b->sm_count) ? (size_t)b->smem_per_sm / 2 + 1024 : 0;
     for (size_t gi = 0; gi < rgroups.size(); ++gi) {
       const ResidentGroup& g = rgroups[gi];
       cudaStream_t st = b->res_streams[gi];
@@ -1385,7 +1398,7 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
       cudaError_t e = cudaStreamWaitEvent(st, b->res_fork, 0);
       if (e == cudaSuccess)
         e = resident_launch(b->storage, b->coll, g.qid, b->d_static, b->d_rdyn + g.first, g.nmem, g.csize, g.stride,
-                            threads, g.parts, st);
+                            threads, g.parts, smem_min, st);
       if (e == cudaSuccess) e = cudaEventRecord(b->res_events[gi], st);
       if (e != cudaSuccess) {
         char what[200];

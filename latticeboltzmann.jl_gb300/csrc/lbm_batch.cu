@@ -26,16 +26,16 @@ cudaError_t batch_launch_q37(int, int, const void*, const BatchDyn*, int, long l
 cudaError_t batch_reduce_q37(int, int, const void*, const ReduceArgs*, const BatchDyn*, int, long long, double*, long long,
                             double*, cudaStream_t);
 
-cudaError_t resident_launch_q4(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
-cudaError_t resident_launch_q5(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
-cudaError_t resident_launch_q9(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
-cudaError_t resident_launch_q13(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
-cudaError_t resident_launch_q17(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
-cudaError_t resident_launch_q21(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
-cudaError_t resident_launch_q37(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
+cudaError_t resident_launch_q4(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
+cudaError_t resident_launch_q5(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
+cudaError_t resident_launch_q9(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
+cudaError_t resident_launch_q13(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
+cudaError_t resident_launch_q17(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
+cudaError_t resident_launch_q21(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
+cudaError_t resident_launch_q37(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
 
 namespace {
-using ResidentFn = cudaError_t (*)(int, int, const void*, const ResidentDyn*, int, int, int, int, int, cudaStream_t);
+using ResidentFn = cudaError_t (*)(int, int, const void*, const ResidentDyn*, int, int, int, int, int, size_t, cudaStream_t);
 const ResidentFn kResident[7] = {resident_launch_q4, resident_launch_q5, resident_launch_q9, resident_launch_q13,
                                  resident_launch_q17, resident_launch_q21, resident_launch_q37};
 using StepFn = cudaError_t (*)(int, int, const void*, const BatchDyn*, int, long long, long long, cudaStream_t);
@@ -64,9 +64,9 @@ cudaError_t batch_reduce_launch(int storage, int qid, int K, const void* statics
 
 // All steps of one call for `nmem` block-resident members of one velocity set (lbm_resident.cuh).
 cudaError_t resident_launch(int storage, int coll, int qid, const void* statics, const ResidentDyn* dyn, int nmem,
-                            int csize, int stride, int threads, int parts, cudaStream_t s) {
+                            int csize, int stride, int threads, int parts, size_t smem_min, cudaStream_t s) {
   if (qid < 0 || qid > 6) return cudaErrorInvalidValue;
-  return kResident[qid](storage, coll, statics, dyn, nmem, csize, stride, threads, parts, s);
+  return kResident[qid](storage, coll, statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
 }
 
 size_t batch_static_size(int storage) {

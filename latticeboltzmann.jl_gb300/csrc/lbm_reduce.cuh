@@ -58,113 +58,132 @@ __device__ __forceinline__ void node_f64(const StepParams<typename S::C>& p, con
   for (int i = 0; i < L::Q; ++i) f[i] = S::DEV ? r.w[i] + (double)v[i] : (double)v[i];
 }
 
+// An FP64 value whose +, - and * are the correctly rounded operations (__dadd_rn, __dsub_rn,
+// __dmul_rn), which the compiler never fuses into FMAs: with plain expressions, whether a product
+// is fused into the sum that consumes it depends on the code around it, so the same reduction could
+// round differently in the single-lattice and the batched kernels that both inline it.  (The oracle,
+// compiled without contraction, rounds every operation too.)
+struct rd {
+  double v;
+  __device__ __forceinline__ rd(double x = 0.0) : v(x) {}
+};
+__device__ __forceinline__ rd operator+(rd a, rd b) { return rd(__dadd_rn(a.v, b.v)); }
+__device__ __forceinline__ rd operator-(rd a, rd b) { return rd(__dsub_rn(a.v, b.v)); }
+__device__ __forceinline__ rd operator*(rd a, rd b) { return rd(__dmul_rn(a.v, b.v)); }
+__device__ __forceinline__ rd operator/(rd a, rd b) { return rd(a.v / b.v); }
+__device__ __forceinline__ rd& operator+=(rd& a, rd b) { return a = a + b; }
+
 // The contribution of node (x, y) to the K sums of one reduction kind.
 template <class L, class S, bool PULL, int K>
 __device__ __forceinline__ void reduce_node(const StepParams<typename S::C>& p, const ReduceArgs& r,
                                             const typename S::T* __restrict__ src, int x, int y, long long node,
                                             double (&acc)[K]) {
+  auto add = [&](int k, rd t) { acc[k] = __dadd_rn(acc[k], t.v); };
   {
-    const double ics = 1.0 / r.cs;
-    double f[L::Q];
-    node_f64<L, S, PULL>(p, r, src, x, y, f);
-    double rho = f[0];
+    const rd ics = 1.0 / r.cs;
+    double fd[L::Q];
+    node_f64<L, S, PULL>(p, r, src, x, y, fd);
+    rd f[L::Q];
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) f[i] = fd[i];
+    rd rho = f[0];
 #pragma unroll
     for (int i = 1; i < L::Q; ++i) rho += f[i];
-    double jx = 0.0, jy = 0.0;
+    rd jx = 0.0, jy = 0.0;
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
-      jx += f[i] * L::cx(i);
-      jy += f[i] * L::cy(i);
+      jx += f[i] * (double)L::cx(i);
+      jy += f[i] * (double)L::cy(i);
     }
-    const double ux = jx / rho, uy = jy / rho;
+    const rd ux = jx / rho, uy = jy / rho;
     if (K == 16) {  // TRACK_ERRORS, track_hydrodynamic_errors.jl:114-203
-      double axx = 0.0, axy = 0.0, ayy = 0.0;  // a_bar_2 = Σ f H_2(c)
+      rd axx = 0.0, axy = 0.0, ayy = 0.0;  // a_bar_2 = Σ f H_2(c)
 #pragma unroll
       for (int i = 0; i < L::Q; ++i) {
-        axx += f[i] * ((double)(L::cx(i) * L::cx(i)) - ics);
+        axx += f[i] * (rd((double)(L::cx(i) * L::cx(i))) - ics);
         axy += f[i] * (double)(L::cx(i) * L::cy(i));
-        ayy += f[i] * ((double)(L::cy(i) * L::cy(i)) - ics);
+        ayy += f[i] * (rd((double)(L::cy(i) * L::cy(i))) - ics);
       }
-      const double exx = rho * (ux * ux), exy = rho * (ux * uy), eyy = rho * (uy * uy);  // a_eq_2, T = 1
+      const rd exx = rho * (ux * ux), exy = rho * (ux * uy), eyy = rho * (uy * uy);  // a_eq_2, T = 1
       const double tau = r.tau;
-      const double h = 1.0 / (2.0 * tau), den = 1.0 + 1.0 / (2.0 * tau);
-      const double A2xx = (axx + h * exx) / den, A2yy = (ayy + h * eyy) / den;
-      const double Pxx = A2xx - rho * (ux * ux - 1.0), Pyy = A2yy - rho * (uy * uy - 1.0);
-      const double pr = (Pxx + Pyy) / 2.0;
+      const rd h = 1.0 / (2.0 * tau), den = 1.0 + 1.0 / (2.0 * tau);
+      const rd A2xx = (axx + h * exx) / den, A2yy = (ayy + h * eyy) / den;
+      const rd Pxx = A2xx - rho * (ux * ux - 1.0), Pyy = A2yy - rho * (uy * uy - 1.0);
+      const rd pr = (Pxx + Pyy) / 2.0;
       // deviatoric_tensor(q, τ, f, ρ, u), moments.jl:81-96
-      const double sxx0 = (axx - exx) / den, sxy0 = (axy - exy) / den, syy0 = (ayy - eyy) / den;
-      const double tr = (sxx0 + syy0) / 2.0;
-      const double fac = 1.0 / (r.u_max * r.u_max);
-      const double sxx = (sxx0 - tr) * fac, sxy = sxy0 * fac, syy = (syy0 - tr) * fac, syx = sxy;
-      const double udx = ux / r.u_max, udy = uy / r.u_max;
+      const rd sxx0 = (axx - exx) / den, sxy0 = (axy - exy) / den, syy0 = (ayy - eyy) / den;
+      const rd tr = (sxx0 + syy0) / 2.0;
+      const rd fac = 1.0 / (r.u_max * r.u_max);
+      const rd sxx = (sxx0 - tr) * fac, sxy = sxy0 * fac, syy = (syy0 - tr) * fac, syx = sxy;
+      const rd udx = ux / r.u_max, udy = uy / r.u_max;
       const size_t k = (size_t)node;
-      const double erho = r.rho_a[k], eux = r.ux_a[k], euy = r.uy_a[k], ep = r.p_a[k];
-      const double esxx = r.sxx_a[k], esyx = r.syx_a[k], esxy = r.sxy_a[k], esyy = r.syy_a[k];
-      acc[0] += (rho - erho) * (rho - erho);
-      acc[1] += (udx - eux) * (udx - eux) + (udy - euy) * (udy - euy);
-      acc[2] += (pr - ep) * (pr - ep);
-      acc[3] += (esxx - sxx) * (esxx - sxx);
-      acc[4] += (esxy - sxy) * (esxy - sxy);
-      acc[5] += (esyy - syy) * (esyy - syy);
-      acc[6] += (esyx - syx) * (esyx - syx);
-      acc[7] += eux * eux + euy * euy;
-      acc[8] += esxx * esxx;
-      acc[9] += esyy * esyy;
-      acc[10] += esxy * esxy;
-      acc[11] += esyx * esyx;
-      acc[12] += ep * ep;
-      acc[13] += rho;
-      acc[14] += rho * (udx + udy);
-      acc[15] += rho * (udx * udx + udy * udy);
+      const rd erho = r.rho_a[k], eux = r.ux_a[k], euy = r.uy_a[k], ep = r.p_a[k];
+      const rd esxx = r.sxx_a[k], esyx = r.syx_a[k], esxy = r.sxy_a[k], esyy = r.syy_a[k];
+      add(0, (rho - erho) * (rho - erho));
+      add(1, (udx - eux) * (udx - eux) + (udy - euy) * (udy - euy));
+      add(2, (pr - ep) * (pr - ep));
+      add(3, (esxx - sxx) * (esxx - sxx));
+      add(4, (esxy - sxy) * (esxy - sxy));
+      add(5, (esyy - syy) * (esyy - syy));
+      add(6, (esyx - syx) * (esyx - syx));
+      add(7, eux * eux + euy * euy);
+      add(8, esxx * esxx);
+      add(9, esyy * esyy);
+      add(10, esxy * esxy);
+      add(11, esyx * esyx);
+      add(12, ep * ep);
+      add(13, rho);
+      add(14, rho * (udx + udy));
+      add(15, rho * (udx * udx + udy * udy));
     } else if (K == 12) {  // COMPARE, processing_methods.jl:177-239
-      double pr;
+      rd pr;
       if (r.q_low_order) {
         pr = 1.0;
       } else {
-        double axx = 0.0, ayy = 0.0;
+        rd axx = 0.0, ayy = 0.0;
 #pragma unroll
         for (int i = 0; i < L::Q; ++i) {
-          axx += f[i] * ((double)(L::cx(i) * L::cx(i)) - ics);
-          ayy += f[i] * ((double)(L::cy(i) * L::cy(i)) - ics);
+          axx += f[i] * (rd((double)(L::cx(i) * L::cx(i))) - ics);
+          ayy += f[i] * (rd((double)(L::cy(i) * L::cy(i))) - ics);
         }
         pr = ((axx + ayy) - rho * ((ux * ux + uy * uy) - 2.0)) / 2.0;  // moments.jl:21-33
       }
-      const double T = pr / rho;
-      const double udx = ux / r.u_max, udy = uy / r.u_max;
-      const double ke = (udx * udx + udy * udy) * rho;
+      const rd T = pr / rho;
+      const rd udx = ux / r.u_max, udy = uy / r.u_max;
+      const rd ke = (udx * udx + udy * udy) * rho;
       const size_t k = (size_t)node;
-      const double erho = r.rho_a[k], ep = r.p_a[k], eux = r.ux_a[k], euy = r.uy_a[k];
-      const double eT = ep / erho, eke = eux * eux + euy * euy;
-      acc[0] += rho;
-      acc[1] += (udx + udy) * rho;
-      acc[2] += ke + T;
-      acc[3] += ke;
-      acc[4] += T;
-      acc[5] += erho;
-      acc[6] += erho * (eux + euy);
-      acc[7] += eke + eT;
-      acc[8] += eke;
-      acc[9] += eT;
-      acc[10] += r.area * ((udx - eux) * (udx - eux) + (udy - euy) * (udy - euy));
-      acc[11] += r.area * ((pr - ep) * (pr - ep));
+      const rd erho = r.rho_a[k], ep = r.p_a[k], eux = r.ux_a[k], euy = r.uy_a[k];
+      const rd eT = ep / erho, eke = eux * eux + euy * euy;
+      add(0, rho);
+      add(1, (udx + udy) * rho);
+      add(2, ke + T);
+      add(3, ke);
+      add(4, T);
+      add(5, erho);
+      add(6, erho * (eux + euy));
+      add(7, eke + eT);
+      add(8, eke);
+      add(9, eT);
+      add(10, rd(r.area) * ((udx - eux) * (udx - eux) + (udy - euy) * (udy - euy)));
+      add(11, rd(r.area) * ((pr - ep) * (pr - ep)));
     } else if (K == 2) {  // MEAN_VELOCITY (stopping_criteria.jl:43-54)
-      acc[0] += ux;
-      acc[1] += 1.0;
+      add(0, ux);
+      add(1, 1.0);
     } else if (K == 3) {  // VELOCITY_CONVERGENCE (stopping_criteria.jl:101-116)
       const size_t k = (size_t)node;
-      const double ox = r.u_old[k], oy = r.u_old[p.n + k];
-      acc[0] += (ux - ox) * (ux - ox) + (uy - oy) * (uy - oy);
-      acc[1] += ox * ox + oy * oy;
-      r.u_old[k] = ux;
-      r.u_old[p.n + k] = uy;
+      const rd ox = r.u_old[k], oy = r.u_old[p.n + k];
+      add(0, (ux - ox) * (ux - ox) + (uy - oy) * (uy - oy));
+      add(1, ox * ox + oy * oy);
+      r.u_old[k] = ux.v;
+      r.u_old[p.n + k] = uy.v;
     } else if (K == 4) {  // CONSERVED
-      acc[0] += rho;
-      acc[1] += jx;
-      acc[2] += jy;
+      add(0, rho);
+      add(1, jx);
+      add(2, jy);
       int bad = 0;
 #pragma unroll
-      for (int i = 0; i < L::Q; ++i) bad += isfinite(f[i]) ? 0 : 1;
-      acc[3] += bad;
+      for (int i = 0; i < L::Q; ++i) bad += isfinite(fd[i]) ? 0 : 1;
+      add(3, (double)bad);
     }
   }
 }

@@ -236,15 +236,16 @@ cudaError_t allow_resident_smem(K kernel, std::atomic<long long>* allowed, size_
 
 template <class L, class S, int COLL, int PARTS>
 cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
-                              int threads, cudaStream_t s) {
+                              int threads, size_t smem_min, cudaStream_t s) {
   auto kernel = resident_step_kernel<L, S, COLL, PARTS>;
   static std::atomic<long long> allowed[64];  // this kernel's shared-memory limit per device
-  const size_t smem = resident_smem_bytes<L, S>(stride);
+  size_t smem = resident_smem_bytes<L, S>(stride);
   if (threads % (32 * PARTS) != 0) return cudaErrorInvalidValue;
   size_t limit = 0;
   cudaError_t e = allow_resident_smem(kernel, allowed, &limit);
   if (e != cudaSuccess) return e;
   if (smem > limit) return cudaErrorInvalidValue;
+  if (smem_min > smem) smem = smem_min < limit ? smem_min : limit;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nmem * csize));
   cfg.blockDim = dim3((unsigned)threads);
@@ -271,41 +272,42 @@ constexpr bool resident_splits() {
 
 template <class L, class S, int COLL>
 cudaError_t resident_launch_c(const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
-                              int threads, int parts, cudaStream_t s) {
+                              int threads, int parts, size_t smem_min, cudaStream_t s) {
   if constexpr ((COLL == LBM_SRT || COLL == LBM_TRT) && resident_splits<L, S>()) {
-    if (parts == 2) return resident_launch_k<L, S, COLL, 2>(statics, dyn, nmem, csize, stride, threads, s);
-    if (parts == 4) return resident_launch_k<L, S, COLL, 4>(statics, dyn, nmem, csize, stride, threads, s);
+    if (parts == 2) return resident_launch_k<L, S, COLL, 2>(statics, dyn, nmem, csize, stride, threads, smem_min, s);
+    if (parts == 4) return resident_launch_k<L, S, COLL, 4>(statics, dyn, nmem, csize, stride, threads, smem_min, s);
   }
   if (parts != 1) return cudaErrorInvalidValue;
-  return resident_launch_k<L, S, COLL, 1>(statics, dyn, nmem, csize, stride, threads, s);
+  return resident_launch_k<L, S, COLL, 1>(statics, dyn, nmem, csize, stride, threads, smem_min, s);
 }
 
 template <class L, class S>
 cudaError_t resident_launch_s(int coll, const void* statics, const ResidentDyn* dyn, int nmem, int csize, int stride,
-                              int threads, int parts, cudaStream_t s) {
+                              int threads, int parts, size_t smem_min, cudaStream_t s) {
   switch (coll) {
-    case LBM_SRT: return resident_launch_c<L, S, LBM_SRT>(statics, dyn, nmem, csize, stride, threads, parts, s);
-    case LBM_TRT: return resident_launch_c<L, S, LBM_TRT>(statics, dyn, nmem, csize, stride, threads, parts, s);
-    case LBM_MRT: return resident_launch_c<L, S, LBM_MRT>(statics, dyn, nmem, csize, stride, threads, parts, s);
+    case LBM_SRT: return resident_launch_c<L, S, LBM_SRT>(statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
+    case LBM_TRT: return resident_launch_c<L, S, LBM_TRT>(statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
+    case LBM_MRT: return resident_launch_c<L, S, LBM_MRT>(statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
 // One resident launch: `nmem` members of velocity set L, each on a cluster of `csize` CTAs of
 // `threads` threads (a multiple of 32 * parts) with `stride` nodes per plane in shared memory, each
-// node's collision split over `parts` warps (1, 2 or 4).
+// node's collision split over `parts` warps (1, 2 or 4).  A CTA asks for at least `smem_min` bytes
+// of shared memory: more than half an SM's keeps every CTA on an SM of its own.
 template <class L>
 cudaError_t resident_launch_set(int storage, int coll, const void* statics, const ResidentDyn* dyn, int nmem,
-                                int csize, int stride, int threads, int parts, cudaStream_t s) {
+                                int csize, int stride, int threads, int parts, size_t smem_min, cudaStream_t s) {
   if (nmem <= 0) return cudaSuccess;
   if (csize < 1 || csize > kResidentMaxCluster || threads < 32 || threads > kResidentThreads) return cudaErrorInvalidValue;
   switch (storage) {
     case LBM_STORE_F64:
-      return resident_launch_s<L, F64>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
+      return resident_launch_s<L, F64>(coll, statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
     case LBM_STORE_DF64_DEV:
-      return resident_launch_s<L, DF64Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
+      return resident_launch_s<L, DF64Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
     case LBM_STORE_F32_DEV:
-      return resident_launch_s<L, F32Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, s);
+      return resident_launch_s<L, F32Dev>(coll, statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -315,7 +317,7 @@ cudaError_t resident_launch_set(int storage, int coll, const void* statics, cons
 #define LBM_RESIDENT_INSTANTIATE(NAME, LAT)                                                                    \
   namespace lbm {                                                                                              \
   cudaError_t resident_launch_##NAME(int storage, int coll, const void* statics, const ResidentDyn* dyn,       \
-                                     int nmem, int csize, int stride, int threads, int parts, cudaStream_t s) { \
-    return resident_launch_set<LAT>(storage, coll, statics, dyn, nmem, csize, stride, threads, parts, s);      \
+                                     int nmem, int csize, int stride, int threads, int parts, size_t smem_min, cudaStream_t s) { \
+    return resident_launch_set<LAT>(storage, coll, statics, dyn, nmem, csize, stride, threads, parts, smem_min, s);      \
   }                                                                                                            \
   }

@@ -580,10 +580,18 @@ __device__ __forceinline__ void collide_pairs(const StepParams<PT>& p, CT* v, CT
     if constexpr (o == i && PART == 0) {
       v[i] = prod_add_out(p.pa_s2, v[i], b0[k]);
     } else if constexpr (o > i && owns_pop<L, PARTS, PART>(i)) {
+      // X = c_i·j': a unit coefficient enters first, so that an integer multiple (|c| = 2, 3) is
+      // added by an explicit FMA rather than a product the compiler may or may not fuse
       CT X;
       bool xs = false;
-      acc_add<L::cx(i)>(X, xs, jx);
-      acc_add<L::cy(i)>(X, xs, jy);
+      constexpr int ax = L::cx(i) < 0 ? -L::cx(i) : L::cx(i), ay = L::cy(i) < 0 ? -L::cy(i) : L::cy(i);
+      if constexpr (ax > 1 && ay == 1) {
+        acc_add<L::cy(i)>(X, xs, jy);
+        acc_add<L::cx(i)>(X, xs, jx);
+      } else {
+        acc_add<L::cx(i)>(X, xs, jx);
+        acc_add<L::cy(i)>(X, xs, jy);
+      }
       [[maybe_unused]] const CT X2 = X * X;
       CT Se = b0[k];
       if constexpr (L::EQ >= 4) Se = add_prod(Se, X2, add_prod(b2[k], X2, b4[k]));
