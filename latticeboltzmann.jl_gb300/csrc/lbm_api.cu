@@ -1385,7 +1385,8 @@ int batch_step_impl(lbm_batch* b, const int64_t* nsteps, const int64_t* t0, cons
     if (cudaEventRecord(b->res_fork, b->stream) != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "resident fork");
     // When every CTA of the call can have an SM of its own, each asks for more than half an SM's
     // shared memory, so that no two share an SM's FP64 units: a small member's step is bound by
-    // the latency of its warps' collision chains, which a second CTA on the SM would lengthen.
+    // the latency of its warps' collision chains, which a second CTA on the SM would lengthen
+    // (a launch whose clusters would not all fit at once that way keeps its own size).
     long long ctas = 0;
     for (const ResidentGroup& g : rgroups) ctas += (long long)g.nmem * g.csize;
     const size_t smem_min = (b->sm_count > 0 && ctas <= b->sm_count) ? (size_t)b->smem_per_sm / 2 + 1024 : 0;

@@ -245,7 +245,6 @@ cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int n
   cudaError_t e = allow_resident_smem(kernel, allowed, &limit);
   if (e != cudaSuccess) return e;
   if (smem > limit) return cudaErrorInvalidValue;
-  if (smem_min > smem) smem = smem_min < limit ? smem_min : limit;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nmem * csize));
   cfg.blockDim = dim3((unsigned)threads);
@@ -258,6 +257,13 @@ cudaError_t resident_launch_k(const void* statics, const ResidentDyn* dyn, int n
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (smem_min > smem) {  // one CTA per SM, if all of this launch's clusters fit that way at once
+    cudaLaunchConfig_t wide = cfg;
+    wide.dynamicSmemBytes = smem_min < limit ? smem_min : limit;
+    int fit = 0;
+    if (cudaOccupancyMaxActiveClusters(&fit, kernel, &wide) == cudaSuccess && fit >= nmem) cfg = wide;
+    else (void)cudaGetLastError();
+  }
   e = cudaLaunchKernelEx(&cfg, kernel, static_cast<const BatchStatic<typename S::C>*>(statics), dyn, csize, stride);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
@@ -295,7 +301,9 @@ cudaError_t resident_launch_s(int coll, const void* statics, const ResidentDyn* 
 // One resident launch: `nmem` members of velocity set L, each on a cluster of `csize` CTAs of
 // `threads` threads (a multiple of 32 * parts) with `stride` nodes per plane in shared memory, each
 // node's collision split over `parts` warps (1, 2 or 4).  A CTA asks for at least `smem_min` bytes
-// of shared memory: more than half an SM's keeps every CTA on an SM of its own.
+// of shared memory -- more than half an SM's keeps every CTA on an SM of its own -- when the
+// device can hold all of the launch's clusters at once that way (cudaOccupancyMaxActiveClusters);
+// otherwise it asks for what its populations need.
 template <class L>
 cudaError_t resident_launch_set(int storage, int coll, const void* statics, const ResidentDyn* dyn, int nmem,
                                 int csize, int stride, int threads, int parts, size_t smem_min, cudaStream_t s) {

@@ -164,15 +164,27 @@ def build_trt_sweep_models(points, scale=1, quadrature="D2Q9", storage="f64"):
     return models, times
 
 
-def run_trt_sweep(points, scale=1, storage="f64", batched=True, sequential_points=None, torch=None):
+def run_trt_sweep(points, scale=1, storage="f64", batched=True, sequential_points=None, torch=None, warmup=True):
     """The sweep batched (simulate_batch over all points) and, for `sequential_points` (a
     subset, or all), one simulate after another.  Both arms build their models first and time
-    the time loops alone (wall clock, synchronised).  Returns rows, timings and runs per second."""
+    the time loops alone (wall clock, synchronised); with `warmup`, a few points run untimed first
+    through each arm, so that the kernels' one-time loading is not timed.  Returns rows, timings
+    and runs per second."""
     from .model import simulate_batch, simulate_model
     if torch is None:
         import torch
     res = {"points": len(points), "scale": scale, "storage": storage}
     rows = {}
+    if warmup:
+        if batched:
+            wm, wt = build_trt_sweep_models(points[:8], scale, storage=storage)
+            simulate_batch(wm, wt)
+            for m in wm:
+                m.close()
+        if sequential_points:
+            wm, wt = build_trt_sweep_models(sequential_points[:1], scale, storage=storage)
+            simulate_model(wm[0], wt[0])
+            wm[0].close()
     if batched:
         t0 = time.perf_counter()
         models, times = build_trt_sweep_models(points, scale, storage=storage)
@@ -306,15 +318,27 @@ def build_shear_wave_study_models(quadratures, tau=0.8, scales=(1, 2, 4, 8), sto
 
 
 def run_shear_wave_study(quadratures=("D2Q4", "D2Q5", "D2Q9", "D2Q13", "D2Q17", "D2Q21", "D2Q37"), tau=0.8,
-                         scales=(1, 2, 4, 8), storage="f64", sequential=True, torch=None):
+                         scales=(1, 2, 4, 8), storage="f64", sequential=True, torch=None, warmup=True):
     """The study batched (simulate_batch: every run in one batch, the time-dependent force of each
     member evaluated at its own step times) and, if `sequential`, once more one simulate after
-    another.  Both arms build their models first and time the time loops alone.  Returns the
-    final rows, timings, and the convergence order of error_u per quadrature."""
+    another.  Both arms build their models first and time the time loops alone; with `warmup`,
+    each arm first runs once untimed on models of its own, so that the kernels' one-time loading
+    is not timed.  Returns the final rows, timings, and the convergence order of error_u per
+    quadrature."""
     from .model import simulate_batch, simulate_model
     if torch is None:
         import torch
     res = {"runs": len(quadratures) * len(scales), "storage": storage, "tau": tau, "scales": list(scales)}
+    if warmup:
+        wm, wt, _ = build_shear_wave_study_models(quadratures, tau, scales, storage)
+        simulate_batch(wm, wt)
+        for m in wm:
+            m.close()
+        if sequential:
+            wm, wt, _ = build_shear_wave_study_models(quadratures, tau, scales, storage)
+            for m, tm in zip(wm, wt):
+                simulate_model(m, tm)
+                m.close()
     models, times, keys = build_shear_wave_study_models(quadratures, tau, scales, storage)
     res["lattice_updates"] = float(sum(m.lattice.nx * m.lattice.ny * (tm.stop - 1) for m, tm in zip(models, times)))
     torch.cuda.synchronize()

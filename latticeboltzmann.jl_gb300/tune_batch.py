@@ -76,7 +76,7 @@ def time_batch(torch, lbm, lats, f0, steps, schedule):
     return best
 
 
-def tune(members=16, steps=200, storages=STORAGES, quads=None, log=sys.stderr):
+def tune(members=8, steps=200, storages=STORAGES, quads=None, log=sys.stderr):
     import numpy as np
     import torch
     lbm = _package()
