@@ -33,7 +33,8 @@ NX = NY = 4096
 Q = 9
 SEED = 20240611
 METRIC = "D2Q9 TRT 4096² MLUPS & %HBM peak: FP64 vs FP32-dev, batched, adjoint"
-BYTES_PER_LU = {"f64": 2 * Q * 8, "df64dev": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2}
+BYTES_PER_LU = {"f64": 2 * Q * 8, "df64dev": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2, "f32sr": 2 * Q * 4}
+ACCURACY_STEPS = 2000  # the configuration's run length, over which each storage's error is measured
 
 
 def tau_from_seed():
@@ -455,7 +456,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev"])
+    ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev", "f32sr"])
     ap.add_argument("--profile", action="store_true",
                     help="time only the device loop of the chosen storage (for profiler runs)")
     ap.add_argument("--case", default="poiseuille", choices=["poiseuille", "mrt_d2q37", "trt_sweep", "adjoint"],
@@ -536,7 +537,16 @@ def main():
 
     extra = {}
     if args.storage == "f64" and rank == 0 and not args.profile:
-        for st in ("df64dev", "f32dev", "f16dev"):
+        # accuracy over the configuration's 2000 steps (untimed): every storage's velocity column
+        # against the FP64 run's
+        ux_acc = {}
+        for st in ("f64", "df64dev", "f32dev", "f16dev", "f32sr"):
+            _, mx, _ = build_model(lbm, st, tau_s)
+            mx.lattice.step(ACCURACY_STEPS, 0, dt)
+            ux_acc[st] = mx.lattice.macroscopic()[1]
+            mx.close()
+        ref_acc = ux_acc["f64"][:, 0]
+        for st in ("df64dev", "f32dev", "f16dev", "f32sr"):
             _, mx, _ = build_model(lbm, st, tau_s)
             sx, _ = time_device(torch, mx, args.steps, args.warmup, dt)
             ux = mx.lattice.macroscopic()[1][:, 0]
@@ -544,7 +554,12 @@ def main():
             extra[st] = {"value": NX * NY * args.steps / sx / 1e6, "unit": "MLUPS", "speedup_vs_f64": seconds / sx,
                          "roofline_frac": BYTES_PER_LU[st] * NX * NY / (sx / args.steps) / 1e9 / peak_gbs,
                          "velocity_error_vs_f64": float(np.max(np.abs(ux - ux_ref)) / np.max(np.abs(ux_ref))),
-                         "error_after_steps": args.warmup + args.steps}
+                         "error_after_steps": args.warmup + args.steps,
+                         f"velocity_error_vs_f64_after_{ACCURACY_STEPS}_steps":
+                             float(np.max(np.abs(ux_acc[st] - ref_acc[:, None])) / np.max(np.abs(ref_acc))),
+                         "error_measure": "max over the lattice of |ux - ux_f64| / max |ux_f64|"}
+        extra["f32sr"]["arithmetic"] = ("FP32 deviation storage, float-float arithmetic, collision outputs stored "
+                                        "with stochastic rounding")
     if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
         extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
                             "batched": bench_batched(torch, lbm), "trt_sweep": bench_trt_sweep(torch, lbm),

@@ -72,8 +72,19 @@ typedef enum { LBM_SRT = 0, LBM_TRT = 1, LBM_MRT = 2, LBM_ITERATIVE_INIT = 3 } l
  *   F16_DEV   g_i in FP16, FP32 arithmetic
  *   DF64_DEV  g_i as a float-float pair (8 bytes, a 48-bit significand on a value far
  *             smaller than f), float-float arithmetic on the FP32 pipes: FP64-class results
- *             at the FP64 storage traffic. */
-typedef enum { LBM_STORE_F64 = 0, LBM_STORE_F32_DEV = 1, LBM_STORE_F16_DEV = 2, LBM_STORE_DF64_DEV = 3 } lbm_storage;
+ *             at the FP64 storage traffic.
+ *   F32_DEV_SR  g_i in FP32 (the F32_DEV traffic), float-float arithmetic, and each collision
+ *             output stored with stochastic rounding (unbiased; a counter-based hash of node,
+ *             population and time index draws the rounding, so runs are reproducible): the
+ *             rounding of a small, steady increment (a body force) no longer accumulates.
+ *             Single lattices only (batches and the adjoint refuse it). */
+typedef enum {
+  LBM_STORE_F64 = 0,
+  LBM_STORE_F32_DEV = 1,
+  LBM_STORE_F16_DEV = 2,
+  LBM_STORE_DF64_DEV = 3,
+  LBM_STORE_F32_DEV_SR = 4
+} lbm_storage;
 
 /* Forcing, applied as the reference does: a velocity shift of the equilibrium, u + τ F
  * (srt.jl:52-54, trt.jl:76-79, mrt.jl:91-95).

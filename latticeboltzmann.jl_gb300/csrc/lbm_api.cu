@@ -216,10 +216,21 @@ int run(lbm_ctx* c, const OpArgs& a) {
   return LBM_OK;
 }
 
-void set_time(lbm_ctx* c, double t) {
+// The physical time of the next eagerly launched step, and its time index (the counter of the
+// stochastic rounding of SR storage).
+void set_time(lbm_ctx* c, double t, int64_t index = 0) {
   c->pd.time = t;
   c->pf.time = t;
   c->px.time = t;
+  c->pd.step_index = index;
+  c->pf.step_index = index;
+  c->px.step_index = index;
+}
+
+// Steps captured into a graph take their time index from the device ({t0, Δt} in c->d_time): for
+// a time-dependent force, and for stochastically rounded storage (its rounding counter).
+bool graph_time(const lbm_ctx* c) {
+  return c->force_kind == LBM_FORCE_SHEAR || c->storage == LBM_STORE_F32_DEV_SR;
 }
 
 // Steps captured into a graph read their time from the device: step k of the graph runs at
@@ -273,7 +284,7 @@ int graph_for_parity(lbm_ctx* c, int parity, cudaGraphExec_t* out) {
     *out = c->graph[parity];
     return LBM_OK;
   }
-  const bool timed = c->force_kind == LBM_FORCE_SHEAR;
+  const bool timed = graph_time(c);
   if (timed && !(c->d_time && c->h_time && c->time_ev)) {  // each part made once, kept if a later one fails
     if ((!c->d_time && !dev_malloc(&c->d_time, 2 * sizeof(long long))) ||
         (!c->h_time && !host_malloc(&c->h_time, 2 * sizeof(long long))))
@@ -367,7 +378,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   if (d->nx < 1 || d->ny < 1 || d->nx >= (int64_t(1) << 31) || d->ny >= (int64_t(1) << 31) ||
       d->nx * d->ny >= (int64_t(1) << 31))
     return LBM_ERR_INVALID;
-  if (d->storage < 0 || d->storage > 3) return LBM_ERR_INVALID;
+  if (d->storage < 0 || d->storage > 4) return LBM_ERR_INVALID;
   if (d->collision < 0 || d->collision > 3) return LBM_ERR_INVALID;
   if (d->force_kind < 0 || d->force_kind > 3) return LBM_ERR_INVALID;
   if (d->nbc < 0 || d->nbc > LBM_MAX_BC || (d->nbc > 0 && !d->bcs)) return LBM_ERR_INVALID;
@@ -388,7 +399,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   c->ny = d->ny;
   c->n = d->nx * d->ny;
   c->elem = (d->storage == LBM_STORE_F64 || d->storage == LBM_STORE_DF64_DEV) ? 8
-            : d->storage == LBM_STORE_F32_DEV ? 4 : 2;
+            : (d->storage == LBM_STORE_F32_DEV || d->storage == LBM_STORE_F32_DEV_SR) ? 4 : 2;
 
   for (int b = 0; b < d->nbc; ++b) {
     const lbm_bc& s = d->bcs[b];
@@ -656,7 +667,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
         drop_reported_error();
         return LBM_ERR_NOMEM;
       }
-    } else if (c->storage == LBM_STORE_DF64_DEV) {
+    } else if (c->storage == LBM_STORE_DF64_DEV || c->storage == LBM_STORE_F32_DEV_SR) {  // float-float arithmetic
       std::vector<dd> tmp(cnt);
       for (size_t k = 0; k < cnt; ++k) tmp[k] = dd(d->nonlinear[k]);
       if (!dev_malloc(&c->d_nonlinear, cnt * sizeof(dd)) ||
@@ -827,12 +838,12 @@ int32_t lbm_step(lbm_ctx* c, int64_t nsteps, int64_t t0, double dt) {
   DeviceGuard device_guard(c->device);
   c->last_launches = 0;
   int64_t k = 0;
-  const bool time_dependent = c->force_kind == LBM_FORCE_SHEAR;
+  const bool time_dependent = graph_time(c);
   const size_t bytes = (size_t)c->n * c->Q * c->elem;
   const bool use_graph = bytes <= kGraphMaxBytes;
-  bool time_uploaded = false;  // time-dependent force: {t0 + k, Δt} on the device for the graphs
+  bool time_uploaded = false;  // graphs with device time: {t0 + k, Δt} on the device for them
   while (k < nsteps) {
-    set_time(c, (double)(t0 + k) * dt);
+    set_time(c, (double)(t0 + k) * dt, t0 + k);
     if (use_graph && c->phase == POST_COLLIDE && nsteps - k >= kGraphSteps) {
       cudaGraphExec_t g = nullptr;
       int rc = graph_for_parity(c, c->cur, &g);
@@ -1148,7 +1159,7 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
     const lbm_ctx* c = members[k];
     if (!c || c->device != c0->device || c->storage != c0->storage || c->coll != c0->coll) return LBM_ERR_INVALID;
     if (c->coll == LBM_ITERATIVE_INIT) return LBM_ERR_UNSUPPORTED;
-    if (c->storage == LBM_STORE_F16_DEV) return LBM_ERR_UNSUPPORTED;
+    if (c->storage == LBM_STORE_F16_DEV || c->storage == LBM_STORE_F32_DEV_SR) return LBM_ERR_UNSUPPORTED;
   }
   {  // a context may appear once: the batch advances each member's own buffers
     std::vector<lbm_ctx*> sorted(members, members + count);

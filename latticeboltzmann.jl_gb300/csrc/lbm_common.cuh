@@ -212,6 +212,7 @@ struct F64 {
   using T = double;     // element in HBM
   using C = double;     // compute type
   static constexpr bool DEV = false;
+  static constexpr bool SR = false;  // collision outputs stored with stochastic rounding
   static constexpr int id = LBM_STORE_F64;
   __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
@@ -221,6 +222,7 @@ struct F32Dev {
   using T = float;
   using C = float;
   static constexpr bool DEV = true;
+  static constexpr bool SR = false;
   static constexpr int id = LBM_STORE_F32_DEV;
   __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
@@ -235,6 +237,7 @@ struct F16Dev {
   using T = __half;
   using C = float;
   static constexpr bool DEV = true;
+  static constexpr bool SR = false;
   static constexpr int id = LBM_STORE_F16_DEV;
   __device__ __forceinline__ static C ld(const T* p) { return __half2float(__ldg(p)); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = __float2half_rn(v); }
@@ -251,6 +254,7 @@ struct DF64Dev {
   using T = float2;
   using C = dd;
   static constexpr bool DEV = true;
+  static constexpr bool SR = false;
   static constexpr int id = LBM_STORE_DF64_DEV;
   __device__ __forceinline__ static C ld(const T* p) {
     const float2 v = __ldg(p);
@@ -265,6 +269,52 @@ struct DF64Dev {
     *reinterpret_cast<float4*>(p) = make_float4(v.hi.lo(), v.lo.lo(), v.hi.hi(), v.lo.hi());
   }
 };
+
+// FP32 deviation storage computed in float-float arithmetic, whose collision outputs are stored
+// with stochastic rounding (st_sr): the float-float value hi + lo becomes hi, or hi's neighbour
+// towards lo, with probability |lo| / (distance to that neighbour), so the stored value is the
+// exact one in expectation.  With round-to-nearest, a small increment (a body force of 1e-6 on
+// deviations of 1e-3) that meets near-identical values every step rounds the same way every step
+// and the error grows linearly in time; unbiased rounding leaves a random walk, which diffusion
+// spreads and averages.  Everything else (uploads, the pull without collision) rounds to nearest.
+struct F32DevSR {
+  using T = float;
+  using C = dd;
+  static constexpr bool DEV = true;
+  static constexpr bool SR = true;
+  static constexpr int id = LBM_STORE_F32_DEV_SR;
+  __device__ __forceinline__ static C ld(const T* p) { return dd(__ldg(p), 0.f); }
+  __device__ __forceinline__ static void st(T* p, C v) { *p = __fadd_rn(v.hi, v.lo); }
+  __device__ __forceinline__ static pdd ld2(const T* p) {
+    pf2 v;
+    v.r = __ldg(reinterpret_cast<const unsigned long long*>(p));
+    return pdd(v, pf2(0.f));
+  }
+};
+
+// 24 uniform bits from (node, population, step): the three are mixed by odd multipliers and the
+// result goes through the "lowbias32" integer finaliser (xor-shift / multiply rounds with the
+// constants C. Wellons published for it).  Counter-based, so a run is reproducible.
+__device__ __forceinline__ unsigned sr_bits(unsigned node, unsigned pop, unsigned step) {
+  unsigned h = node * 0x9E3779B9u ^ (pop + 1u) * 0x85EBCA6Bu ^ (step + 0x632BE5ABu) * 0xC2B2AE35u;
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  return h >> 8;
+}
+
+// Stochastic rounding of a normalised float-float value (|lo| at most half an ulp of hi) to a
+// float, with the 24 uniform bits u: the neighbour n of hi towards lo is taken when
+// u 2^-24 |n - hi| < |lo|.  |n - hi| is a power of two, so the comparison is exact.
+__device__ __forceinline__ float round_stochastic(float hi, float lo, unsigned u) {
+  if (lo == 0.f || hi == 0.f || !isfinite(hi)) return __fadd_rn(hi, lo);
+  const int b = __float_as_int(hi);
+  const float n = __int_as_float(b + (((lo > 0.f) == (hi > 0.f)) ? 1 : -1));
+  const float gap = fabsf(__fsub_rn(n, hi));
+  return __fmul_rn(__fmul_rn((float)u, gap), 0x1p-24f) < fabsf(lo) ? n : hi;
+}
 
 // ---------------------------------------------------------------------------------------
 // Kernel parameter blocks (passed by value; they live in the constant bank).
@@ -304,6 +354,8 @@ struct StepParams {
   double time;                 // physical time of this step
   const long long* time_base;  // when set: {t0, bits of Δt} on the device, and the step runs at
   int time_step;               // time (t0 + time_step) Δt (steps of a CUDA graph, see step_time)
+  long long step_index;        // time index of this step when time_base is not set (the counter of
+                               // stochastic rounding, step_counter)
   const CT* nonlinear;         // ITER: nonlinear equilibrium term planes (device)
   int nbc;
   BCDev bc[LBM_MAX_BC];

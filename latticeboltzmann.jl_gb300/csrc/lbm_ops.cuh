@@ -49,9 +49,10 @@ inline void launch_step(const OpArgs& a, const StepParams<typename S::C>& p) {
   auto* dst = static_cast<typename S::T*>(a.dst);
   // SRT / TRT of the deviation storages: two nodes per thread on packed FP32 pairs (even nx).
   // Where the pair kernel's registers would cut the occupancy too far, the one-node kernel stays:
-  // D2Q37 in FP32 / FP16 (154 registers against 72, measured 8 % slower), and float-float above
-  // D2Q9 (D2Q13: 126 against 56).
-  constexpr bool kPairs = MODE == 1 && S::DEV && (S::id == LBM_STORE_DF64_DEV ? L::Q <= 9 : L::Q <= 25);
+  // D2Q37 in FP32 / FP16 (154 registers against 72, measured 8 % slower), and float-float
+  // arithmetic (DF64 and FP32-SR storage) above D2Q9 (D2Q13: 126 against 56).
+  constexpr bool kPairs =
+      MODE == 1 && S::DEV && (std::is_same<typename S::C, dd>::value ? L::Q <= 9 : L::Q <= 25);
   if constexpr (kPairs) {
     if ((a.coll == LBM_SRT || a.coll == LBM_TRT) && p.nx % 2 == 0) {
       const dim3 g2((unsigned)((p.nx / 2 + kBlockX - 1) / kBlockX), g.y);
@@ -156,6 +157,7 @@ cudaError_t run_op(const OpArgs& a) {
     case LBM_STORE_F32_DEV: return run_op_s<L, F32Dev>(a, *a.pf);
     case LBM_STORE_F16_DEV: return run_op_s<L, F16Dev>(a, *a.pf);
     case LBM_STORE_DF64_DEV: return run_op_s<L, DF64Dev>(a, *a.px);
+    case LBM_STORE_F32_DEV_SR: return run_op_s<L, F32DevSR>(a, *a.px);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -127,6 +127,22 @@ __device__ __forceinline__ double step_time(const StepParams<CT>& p) {
   return (double)(p.time_base[0] + p.time_step) * __longlong_as_double(p.time_base[1]);
 }
 
+// Counter of the stochastic rounding of SR storages: the time index of the step (the graph's t0 +
+// its step number, or the index the host set for an eager launch).
+template <class CT>
+__device__ __forceinline__ unsigned step_counter(const StepParams<CT>& p) {
+  return (unsigned)(p.time_base ? p.time_base[0] + p.time_step : p.step_index);
+}
+
+// Stores collision output i of node `node`: stochastically rounded for an SR storage (F32DevSR),
+// else as S::st.
+template <class S, class CT>
+__device__ __forceinline__ void store_out(const StepParams<CT>& p, typename S::T* dst, int i, int node,
+                                          typename S::C v) {
+  if constexpr (S::SR) dst[plane_off(p, i) + node] = round_stochastic(v.hi, v.lo, sr_bits(node, i, step_counter(p)));
+  else S::st(dst + plane_off(p, i) + node, v);
+}
+
 // Lattice force at node (x, y), lattice_force(problem, x, y, t) (problems.jl:103-104).  `time()`
 // gives the physical time of the step; it is called only for the time-dependent force, so the
 // steps of the other forces spend no FP64 instruction on it.
@@ -658,7 +674,7 @@ constexpr int kBlockX = 128;
 // (left alone the compiler takes 96 and spills), 6.6 against 6.2 GLUPS on the 2048^2 shear wave;
 // a bound of 6 blocks (80 registers, 84 bytes spilled) ran at 6.1.
 template <class L, class S, int COLL, int MODE>
-__global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && S::id == LBM_STORE_DF64_DEV && L::Q == 37) ? 4 : 0) step_kernel(StepParams<typename S::C> p,
+__global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STORE_DF64_DEV || S::id == LBM_STORE_F32_DEV_SR) && L::Q == 37) ? 4 : 0) step_kernel(StepParams<typename S::C> p,
                                                        const typename S::T* __restrict__ src,
                                                        typename S::T* __restrict__ dst) {
   using CT = typename S::C;
@@ -673,7 +689,7 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && S::id == LBM_STOR
       CT sFx = 0, sFy = 0;
       const bool has_force = p.force_kind != LBM_FORCE_NONE;
       if (has_force) node_shifted_force(p, x, y, sFx, sFy, [&] { return step_time(p); });
-      auto out = [&](int i, CT val) { S::st(dst + plane_off(p, i) + node, val); };
+      auto out = [&](int i, CT val) { store_out<S>(p, dst, i, node, val); };
       if constexpr (MODE == 0) {
         mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
                             [&](auto I) { return S::ld(src + plane_off(p, decltype(I)::value) + node); }, out);
@@ -696,9 +712,14 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && S::id == LBM_STOR
       CT v[L::Q];
       if (MODE == 0) load_local<L, S>(p, src, node, v);
       else load_streamed<L, S>(p, src, x, y, v);
-      if (MODE != 2) collide_node<L, S, COLL>(p, x, y, v, [&] { return step_time(p); });
+      if (MODE != 2) {
+        collide_node<L, S, COLL>(p, x, y, v, [&] { return step_time(p); });
 #pragma unroll
-      for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
+        for (int i = 0; i < L::Q; ++i) store_out<S>(p, dst, i, node, v[i]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
+      }
     }
   }
 }
@@ -756,7 +777,16 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
     }
     collide_pairs<L, S::DEV>(p, v, sFx, sFy, has_force);
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) S::st2(dst + plane_off(p, i) + node, v[i]);
+    for (int i = 0; i < L::Q; ++i) {
+      if constexpr (S::SR) {  // both lanes stochastically rounded, stored as one two-node access
+        const unsigned step = step_counter(p);
+        const float a = round_stochastic(v[i].hi.lo(), v[i].lo.lo(), sr_bits(node, i, step));
+        const float b = round_stochastic(v[i].hi.hi(), v[i].lo.hi(), sr_bits(node + 1, i, step));
+        *reinterpret_cast<unsigned long long*>(dst + plane_off(p, i) + node) = pf2(a, b).r;
+      } else {
+        S::st2(dst + plane_off(p, i) + node, v[i]);
+      }
+    }
   }
 }
 

@@ -43,9 +43,11 @@ def _force_descriptor(cm, q, problem):
 class LatticeBoltzmannModel:
     """LatticeBoltzmannModel(problem, q; collision_model=SRT, initialization_strategy, process_method)
     with the populations resident on the GPU.  `storage` selects FP64 ("f64"), the float-float
-    deviation storage ("df64dev", FP64-class, FP32 pipes) or the FP32 / FP16 deviation storage
-    ("f32dev" / "f16dev").  Closed-form initial conditions are built on the device from their
-    macroscopic planes unless `device_init` is False or `f0` (shape (Q, NY, NX)) is given."""
+    deviation storage ("df64dev", FP64-class, FP32 pipes), the FP32 / FP16 deviation storage
+    ("f32dev" / "f16dev"), or the FP32 deviation storage with float-float arithmetic and
+    stochastically rounded stores ("f32sr").  Closed-form initial conditions are built on the
+    device from their macroscopic planes unless `device_init` is False or `f0` (shape (Q, NY, NX))
+    is given."""
 
     def __init__(self, problem, quadrature, collision_model=SRT, initialization_strategy=None,
                  process_method=None, storage="f64", f0=None, device_init=True):

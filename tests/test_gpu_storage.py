@@ -1,4 +1,5 @@
-"""FP32 / FP16 deviation storage (g = f - w, FP32 arithmetic) against the FP64 path."""
+"""FP32 / FP16 deviation storage (g = f - w, FP32 arithmetic), and FP32 deviation storage with
+float-float arithmetic and stochastically rounded stores, against the FP64 path."""
 import numpy as np
 import pytest
 
@@ -65,3 +66,68 @@ def test_deviation_storage_with_walls_and_force(lbm_gpu, O, storage):
     ux64 = res["f64"][1]
     rel = float(np.max(np.abs(res[storage][1] - ux64)) / np.max(np.abs(ux64)))
     assert rel < (1e-5 if storage == "f32dev" else 5e-2), rel
+
+
+# ---- FP32 deviation storage with float-float arithmetic and stochastically rounded stores ----
+
+@pytest.mark.parametrize("qname", QUADS)
+@pytest.mark.parametrize("coll", ["SRT", "TRT", "MRT"])
+def test_f32sr_matches_f64(lbm_gpu, qname, coll):
+    lbm = lbm_gpu
+    q = lbm.Quadratures[qname]
+    f0 = wave_field(q, 48, 40, seed=11, amp=0.01)
+    cm = {"SRT": lbm.SRT(0.8), "TRT": lbm.TRT.fields(0.8, 1.0), "MRT": lbm.MRT(q, 0.8)}[coll]
+    out = {}
+    for storage in ("f64", "f32sr"):
+        m = lbm.LatticeBoltzmannModel.from_parts(q, f0, cm, storage=storage)
+        m.lattice.step(200, 0, 0.0)
+        out[storage] = _velocity(lbm, m)
+        m.close()
+    u64 = np.hypot(out["f64"][1], out["f64"][2])
+    du = np.hypot(out["f32sr"][1] - out["f64"][1], out["f32sr"][2] - out["f64"][2])
+    assert float(du.max() / u64.max()) < 1e-5
+    assert float(np.max(np.abs(out["f32sr"][0] - out["f64"][0]))) < 1e-6
+
+
+def test_f32sr_is_reproducible(lbm_gpu):
+    """The rounding is drawn from a hash of (node, population, time index): the same run twice
+    gives the same bits, and the same steps issued eagerly or from captured graphs agree."""
+    lbm = lbm_gpu
+    q = lbm.D2Q9()
+    f0 = wave_field(q, 40, 30, seed=5, amp=0.01)
+    res = []
+    for split in ((150,), (150,), (1,) * 150):
+        m = lbm.LatticeBoltzmannModel.from_parts(q, f0, lbm.TRT.fields(0.8, 1.1), force=("constant", (1e-6, 0.0)),
+                                                 storage="f32sr")
+        t = 0
+        for n in split:
+            m.lattice.step(n, t, 0.0)
+            t += n
+        res.append(m.f_stream)
+        m.close()
+    assert np.array_equal(res[0], res[1])
+    assert np.array_equal(res[0], res[2])
+
+
+def test_f32sr_forced_channel_velocity_error(lbm_gpu):
+    """The benchmark's forced channel (D2Q9 TRT, magic Λ = 1/4, 4096 x 4096, walls North / South,
+    lattice force 1e-6, τ_s from the benchmark's seed) for its 2000 steps: the FP32-deviation
+    storage with stochastic rounding stays within 1e-6 relative velocity error of the FP64 run,
+    where round-to-nearest FP32 arithmetic and storage drift to ~5e-5."""
+    lbm = lbm_gpu
+    tau_s = float(np.random.default_rng(20240611).uniform(0.55, 1.5))
+    q = lbm.D2Q9()
+    n, steps = 4096, 2000
+    res = {}
+    for storage in ("f64", "f32sr"):
+        problem = lbm.PoiseuilleFlow.fields(1.0, 0.05, (tau_s - 0.5) / 3.0, n, n, 1.0, (1.0, 1.0), 1.0)
+        problem.G = 1e-6 / (0.05 * problem.delta_t() * problem.viscosity())
+        cm = lbm.TRT.fields(tau_s, 0.5 + 0.25 / (tau_s - 0.5), "problem")
+        m = lbm.LatticeBoltzmannModel(problem, q, collision_model=cm, storage=storage,
+                                      initialization_strategy=lbm.ZeroVelocityInitialCondition())
+        lbm.run_steps(m, 0, steps - 1)
+        res[storage] = m.lattice.macroscopic()[1]
+        m.close()
+    ref = res["f64"][:, 0]
+    rel = float(np.max(np.abs(res["f32sr"] - ref[:, None])) / np.max(np.abs(ref)))
+    assert rel <= 1e-6, rel
