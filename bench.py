@@ -358,7 +358,7 @@ def bench_adjoint(torch, lbm, n=512, steps=4000):
     q = lbm.D2Q9()
     tau_s = 0.8
     out = {"workload": f"adjoint of D2Q9 TRT {n}x{n} periodic, {steps} steps, loss = |u_T - u*|^2, "
-                       "divergence-free Fourier start (k <= 8, amplitude 0.01), sqrt(T) checkpointing"}
+                       "divergence-free Fourier start (k <= 8, amplitude 0.01), binomial checkpointing"}
     u0 = lbm.divergence_free_field(n, n, 8, 0.01, seed=11)
     ut = lbm.divergence_free_field(n, n, 8, 0.01, seed=12)
     for st in ("f32dev",):
@@ -369,10 +369,29 @@ def bench_adjoint(torch, lbm, n=512, steps=4000):
         t0 = time.perf_counter()
         res = prob.run(u0, ut)
         t1 = time.perf_counter()
+        info = prob.info()
         prob.close()
         out[st] = {"seconds": t1 - t0, "forward_equivalent_mlups": n * n * steps / (t1 - t0) / 1e6,
                    "loss": res["loss"], "dL_dtau_s_total": lbm.magic_total_derivative(res, tau_s),
-                   "dL_dF": [float(x) for x in res["dF"]]}
+                   "dL_dF": [float(x) for x in res["dF"]], "checkpoint_slots": info["slots"],
+                   "forward_steps": info["forward_steps"], "device_bytes": info["device_bytes"],
+                   "state_bytes": n * n * 9 * 4}
+    # a memory budget: 8 slots instead of the default (every step recomputed at most r times,
+    # C(8 + r, 8) >= T), and the walled channel (bounce-back North / South)
+    for label, kw in (("f32dev_8_slots", {"slots": 8}),
+                      ("f32dev_channel_walls", {"boundary_conditions": [lbm.BounceBack(lbm.North(), (1, n), (1, n)),
+                                                                        lbm.BounceBack(lbm.South(), (1, n), (1, n))]})):
+        prob = lbm.AdjointProblem(q, n, n, lbm.TRT.fields(tau_s, lbm.trt_magic(tau_s)), force=(1e-6, 0.0),
+                                  nsteps=steps, storage="f32dev", **kw)
+        prob.run(u0, ut, want_grad_u0=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = prob.run(u0, ut)
+        t1 = time.perf_counter()
+        info = prob.info()
+        prob.close()
+        out[label] = {"seconds": t1 - t0, "loss": res["loss"], "checkpoint_slots": info["slots"],
+                      "forward_steps": info["forward_steps"], "device_bytes": info["device_bytes"]}
     return out
 
 

@@ -296,17 +296,23 @@ int32_t lbm_batch_share_stream(lbm_batch* batch);
 
 /* ---- adjoint (reverse-mode gradients) -----------------------------------------------------
  * No differentiation exists in the reference; this is the discrete adjoint of the fused step
- * for periodic D2Q9 / D2Q13 lattices with SRT or TRT and a uniform force (the context's
- * descriptor), FP64 or FP32-deviation storage.  For the loss
- *   L = Σ_x |u(f_T) - u*|²,  f_0 = f_eq(ρ = 1, u0),  f_{t+1} = stream(collide(f_t)),  T = nsteps,
+ * for D2Q9 / D2Q13 lattices with SRT or TRT, a uniform force and the context's boundary
+ * conditions (bounce-back on any side, moving wall: the pull's transpose swaps opposite
+ * populations at the walls), FP64 or FP32-deviation storage.  For the loss
+ *   L = Σ_x |u(f_T) - u*|²,  f_0 = f_eq(ρ = 1, u0),  f_{t+1} = apply!(stream(collide(f_t))),  T = nsteps,
  * lbm_adjoint_run returns result[0] = L, result[1] = ∂L/∂τ_s (SRT: dL/dτ), result[2] = ∂L/∂τ_a
  * (TRT; 0 for SRT), result[3..4] = ∂L/∂F, and, if grad_u0 is not NULL, ∂L/∂u0 as two planes of
- * nx*ny (Julia layout, like u0 and u_target).  Memory is bounded by checkpointing: the state
- * entering every checkpoint_every-th step is kept (0 selects ⌈√nsteps⌉) and each segment is
- * recomputed once during the reverse sweep; the whole forward + reverse sweep is one CUDA graph.
- * Loss and parameter sums are FP64, in a fixed order. */
+ * nx*ny (Julia layout, like u0 and u_target).  Memory is bounded by binomial checkpointing
+ * (Griewank's schedule): `slots` lattice states are kept (0 selects the fewest with which no
+ * forward step is recomputed more than twice), and the reverse sweep recomputes the states it
+ * needs from them; with s slots and r = the least count such that C(s + r, s) >= nsteps, no step
+ * is recomputed more than r times.  The whole forward + reverse sweep is one CUDA graph.  Loss and
+ * parameter sums are FP64, in a fixed order. */
 typedef struct lbm_adjoint lbm_adjoint;
-int32_t lbm_adjoint_create(lbm_adjoint** adjoint, lbm_ctx* ctx, int64_t nsteps, int64_t checkpoint_every);
+int32_t lbm_adjoint_create(lbm_adjoint** adjoint, lbm_ctx* ctx, int64_t nsteps, int64_t slots);
+/* The schedule's checkpoint slots, its forward steps (nsteps without checkpointing) and the device
+ * memory the adjoint holds, in bytes (any pointer may be NULL). */
+int32_t lbm_adjoint_info(const lbm_adjoint* adjoint, int64_t* slots, int64_t* forward_steps, int64_t* device_bytes);
 void lbm_adjoint_destroy(lbm_adjoint* adjoint);
 int32_t lbm_adjoint_run(lbm_adjoint* adjoint, const double* u0, const double* u_target, double* result,
                         double* grad_u0);

@@ -140,6 +140,8 @@ def lib():
         L.lbm_batch_set_schedule.restype = C.c_int32
         L.lbm_adjoint_create.argtypes = [C.POINTER(vp), vp, C.c_int64, C.c_int64]
         L.lbm_adjoint_create.restype = C.c_int32
+        L.lbm_adjoint_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.lbm_adjoint_info.restype = C.c_int32
         L.lbm_adjoint_destroy.argtypes = [vp]
         L.lbm_adjoint_destroy.restype = None
         L.lbm_adjoint_run.argtypes = [vp, _DP, _DP, _DP, _DP]
@@ -156,7 +158,7 @@ EXPORTED_SYMBOLS = [
     "lbm_download_device", "lbm_step", "lbm_last_launch_count", "lbm_reduce", "lbm_macroscopic",
     "lbm_collide_device", "lbm_stream_device", "lbm_apply_bcs_device", "lbm_batch_create", "lbm_batch_destroy",
     "lbm_batch_step", "lbm_batch_step_timed", "lbm_batch_set_stream", "lbm_batch_synchronize", "lbm_batch_last_launch_count",
-    "lbm_batch_last_error", "lbm_batch_reduce", "lbm_batch_reduce_fields", "lbm_batch_share_stream", "lbm_batch_set_schedule", "lbm_initialize_fields", "lbm_adjoint_create", "lbm_adjoint_destroy", "lbm_adjoint_run",
+    "lbm_batch_last_error", "lbm_batch_reduce", "lbm_batch_reduce_fields", "lbm_batch_share_stream", "lbm_batch_set_schedule", "lbm_initialize_fields", "lbm_adjoint_create", "lbm_adjoint_info", "lbm_adjoint_destroy", "lbm_adjoint_run",
     "lbm_adjoint_last_error",
 ]
 

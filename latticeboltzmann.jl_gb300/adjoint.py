@@ -2,12 +2,12 @@
 
 The reference has no differentiation (no ForwardDiff / ChainRulesCore in its manifests, and its
 SRT hard-types τ as Float64).  This module exposes the discrete adjoint of the device kernels for
-periodic D2Q9 / D2Q13 lattices with SRT or TRT and a uniform force:
+D2Q9 / D2Q13 lattices with SRT or TRT, a uniform force and bounce-back / moving-wall boundaries:
 
-    L(u0, τ, F) = Σ_x |u(f_T) - u*|²,   f_0 = f_eq(1, u0),   f_{t+1} = stream(collide(f_t; τ, F)),
+    L(u0, τ, F) = Σ_x |u(f_T) - u*|²,   f_0 = f_eq(1, u0),   f_{t+1} = apply!(stream(collide(f_t; τ, F))),
 
-`AdjointProblem.run(u0, u_target)` returns L, ∂L/∂τ_s, ∂L/∂τ_a, ∂L/∂F and ∂L/∂u0 (√T
-checkpointing, one CUDA graph).  `LBMLoss` wraps it as a torch.autograd.Function, the Python
+`AdjointProblem.run(u0, u_target)` returns L, ∂L/∂τ_s, ∂L/∂τ_a, ∂L/∂F and ∂L/∂u0 (binomial
+checkpointing with a given number of state slots, one CUDA graph).  `LBMLoss` wraps it as a torch.autograd.Function, the Python
 counterpart of a ChainRulesCore.rrule for `simulate`.
 """
 from __future__ import annotations
@@ -22,18 +22,30 @@ from .device import DeviceLattice
 
 
 class AdjointProblem:
-    def __init__(self, q, nx, ny, collision_model, force=(0.0, 0.0), nsteps=100, checkpoint_every=0,
-                 storage="f64"):
+    """The adjoint of `nsteps` steps of an nx x ny lattice.  `boundary_conditions` are BounceBack /
+    MovingWall instances (applied in list order after the stream, as in the forward model);
+    `slots` is the number of lattice states kept for the binomial checkpointing schedule (0: the
+    fewest with which no step is recomputed more than twice)."""
+
+    def __init__(self, q, nx, ny, collision_model, force=(0.0, 0.0), nsteps=100, slots=0, storage="f64",
+                 boundary_conditions=()):
         self.q, self.nx, self.ny, self.nsteps = q, int(nx), int(ny), int(nsteps)
         self.collision_model = collision_model
         self.force = (float(force[0]), float(force[1]))
         dev_force = ("constant", self.force) if any(self.force) else None
-        self.lattice = DeviceLattice(q, nx, ny, collision_model, (), force=dev_force, storage=storage)
+        self.lattice = DeviceLattice(q, nx, ny, collision_model, tuple(boundary_conditions), force=dev_force,
+                                     storage=storage)
         h = C.c_void_p()
-        st = N.lib().lbm_adjoint_create(C.byref(h), self.lattice.h, self.nsteps, int(checkpoint_every))
+        st = N.lib().lbm_adjoint_create(C.byref(h), self.lattice.h, self.nsteps, int(slots))
         if st != N.LBM_OK:
             raise N.LbmError(st, N.lib().lbm_last_error(self.lattice.h).decode())
         self.h = h
+
+    def info(self):
+        """{"slots", "forward_steps", "device_bytes"} of the checkpointing schedule."""
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        N.check(None, N.lib().lbm_adjoint_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"slots": a.value, "forward_steps": b.value, "device_bytes": c.value}
 
     def run(self, u0, u_target, want_grad_u0=True):
         """u0, u_target: arrays of shape (2, NY, NX).  Returns a dict with the loss and gradients."""

@@ -1,13 +1,16 @@
 // lbm_adjoint.cuh -- reverse-mode (adjoint) kernels of the fused collide-stream step.
 //
 // The reference has no differentiation; this is the discrete adjoint of the forward map the
-// kernels implement, for periodic lattices with SRT or TRT collision and a uniform force:
+// kernels implement, for lattices with SRT or TRT collision, a uniform force and the boundary
+// conditions (bounce-back, moving wall):
 //
 //   A_{t+1} = S C(A_t; τ_s, τ_a, F),  A_0 = f_eq(ρ = 1, u0),  L = Σ_x |u(A_T) - u*|²,
 //
-// with S the periodic pull (a permutation) and C the per-node collision.  The adjoint state
-// λ_t = ∂L/∂A_t obeys λ_t = J_C(A_t)^T S^T λ_{t+1}: S^T is the pull in the opposite direction
-// (λ from x + c_i), and J_C^T is applied per node in O(Q):
+// with S the periodic pull followed by the boundary rules (each population taken from one source:
+// a neighbour, or the same node's opposite population where a wall replaces it; a moving wall adds
+// a constant) and C the per-node collision.  The adjoint state λ_t = ∂L/∂A_t obeys
+// λ_t = J_C(A_t)^T S^T λ_{t+1}: S^T sends each λ back to its population's source (λ from x + c_i,
+// and at a wall the swap of opposite populations), and J_C^T is applied per node in O(Q):
 //
 //   C(f) = M f + N f_eq(ρ(f), u'(f)),   M = (1-ω_s) P_s + (1-ω_a) P_a,   N = ω_s P_s + ω_a P_a,
 //   J_C^T μ = M μ + (∂f_eq/∂f)^T ν,  ν = N μ,
@@ -128,6 +131,31 @@ __global__ void __launch_bounds__(kAdjThreads) adj_loss_kernel(StepParams<typena
   adj_block_add<1>(acc, slots);
 }
 
+// Whether the boundary conditions replace population i of node (x, y) in the pull (the rule of
+// load_streamed: bounce_back.jl:8-72, moving_wall.jl:17-38).  A replaced population is the same
+// node's post-collision opposite population (plus a constant for a moving wall), whichever of the
+// listed conditions replaces it last.
+template <class L, class CT>
+__device__ __forceinline__ bool bc_replaces(const StepParams<CT>& p, int x, int y, int i) {
+  const int o = L::opp(i);
+  const int y1 = y + 1, x1 = x + 1;
+  for (int b = 0; b < p.nbc; ++b) {
+    const BCDev& bc = p.bc[b];
+    if (bc.kind == LBM_BOUNCE_BACK) {
+      if (x < bc.x_lo || x > bc.x_hi || y < bc.y_lo || y > bc.y_hi) continue;
+      bool hit;
+      if (bc.dir == LBM_NORTH) hit = y1 + L::cy(o) > p.ny;
+      else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
+      else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
+      else hit = x1 + L::cx(o) <= 0;
+      if (hit) return true;
+    } else if (y1 + L::cy(o) > p.ny) {
+      return true;
+    }
+  }
+  return false;
+}
+
 // One reverse step: λ_t = J_C(A_t)^T S^T λ_{t+1}.  A_t is pulled from B_{t-1} (pull = true) or
 // read locally (A_0).  Parameter sensitivities are added to this block's slots.
 template <class L, class S, int COLL>
@@ -153,14 +181,30 @@ __global__ void __launch_bounds__(kAdjThreads, (S::DEV && L::Q <= 9) ? 4 : 1) ad
     CT f[L::Q];
     if (pull) load_streamed<L, S>(p, src, x, y, f);
     else load_local<L, S>(p, src, (int)node, f);
-    // μ = S^T λ_{t+1}: λ from x + c_i (the opposite of the forward pull)
+    // μ = S^T λ_{t+1}: λ from x + c_i (the opposite of the forward pull).  With boundary
+    // conditions, population i of x + c_i pulls from x only where no condition replaces it, and a
+    // population replaced at x itself (the opposite of i, read from this node) sends its λ here;
+    // both can only happen within 2R of an edge.
     CT mu[L::Q];
     {
       int xw[2 * L::R + 1], yo[2 * L::R + 1];
       pull_offsets<L>(p, x, y, xw, yo);
+      const bool near = p.nbc > 0 && (y < 2 * L::R || y >= p.ny - 2 * L::R || x < 2 * L::R || x >= p.nx - 2 * L::R);
       static_for<0, L::Q>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        mu[i] = (CT)lam_next[(size_t)i * p.n + yo[L::R - L::cy(i)] + xw[L::R - L::cx(i)]];
+        const size_t from = (size_t)i * p.n + yo[L::R - L::cy(i)] + xw[L::R - L::cx(i)];
+        if (!near) {
+          mu[i] = (CT)lam_next[from];
+        } else {
+          int xt = x - p.dxm[3 - L::cx(i)], yt = y - p.dym[3 - L::cy(i)];  // x + c_i, periodic
+          xt += xt < 0 ? p.nx : 0;
+          yt += yt < 0 ? p.ny : 0;
+          CT m = 0;
+          if (!bc_replaces<L>(p, xt, yt, i)) m = (CT)lam_next[from];
+          constexpr int o = L::opp(i);
+          if (bc_replaces<L>(p, x, y, o)) m = m + (CT)lam_next[(size_t)o * p.n + (size_t)y * p.nx + x];
+          mu[i] = m;
+        }
       });
     }
     // moments, equilibrium and its velocity derivatives (as the forward collision forms them)

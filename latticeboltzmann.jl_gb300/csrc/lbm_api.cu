@@ -1715,15 +1715,25 @@ int32_t lbm_batch_reduce_fields(lbm_batch* b, int32_t kind, const uint8_t* selec
 
 // ---- adjoint -------------------------------------------------------------------------------
 
+// One action of the adjoint's plan.  A location names a state buffer: kLocA0 (A_0), kLocWork + w
+// (two work buffers) or a checkpoint slot (>= 0).
+struct AdjAction {
+  enum Kind { FWD, LOSS, ADJ } kind;
+  int src, dst;  // FWD: src -> dst (one step); LOSS: src holds B_{T-1}; ADJ: src holds the state entering t
+  int64_t t;     // FWD: the step's time index (0: the collision-only first step); ADJ: the reversed step
+};
+constexpr int kLocA0 = -1, kLocWork = -3;  // work buffers: kLocWork + 0, kLocWork + 1 (= -3, -2)
+
 struct lbm_adjoint {
   lbm_ctx* ctx = nullptr;
-  int64_t T = 0, k = 0, nck = 0;
+  int64_t T = 0, nslots = 0;
   size_t bytes = 0;
   int nblocks = 0;
   void* a0 = nullptr;
-  void* fwd[2] = {nullptr, nullptr};
-  std::vector<void*> ckpt;  // ckpt[c] = B_{c k - 1}, the state entering step c k (c >= 1)
-  std::vector<void*> seg;   // recomputed B_t inside one segment
+  void* work[2] = {nullptr, nullptr};
+  std::vector<void*> slot;      // checkpoints of the binomial schedule
+  std::vector<AdjAction> plan;  // the forward, loss and reverse steps, in order
+  int64_t forward_steps = 0;    // forward steps of the plan (T without checkpointing)
   void* lam[2] = {nullptr, nullptr};
   double* d_u0 = nullptr;
   double* d_ut = nullptr;
@@ -1738,6 +1748,79 @@ struct lbm_adjoint {
 
 namespace {
 
+// β(s, r) = C(s + r, s): the most steps that s checkpoints reverse with every step recomputed at
+// most r times (Griewank, "Achieving logarithmic growth of temporal and spatial complexity in
+// reverse automatic differentiation", 1992), saturated at 2^62.
+int64_t binomial_beta(int64_t s, int64_t r) {
+  double b = 1.0;
+  for (int64_t j = 1; j <= s; ++j) {
+    b = b * (double)(r + j) / (double)j;
+    if (b > 4.6e18) return int64_t(1) << 62;
+  }
+  return (int64_t)(b + 0.5);
+}
+
+// The plan of the binomial (revolve-type) checkpointing schedule.  reverse(start, t0, t1, s):
+// the state entering step t0 is at `start`, λ_{t1} is known (or, on the rightmost path, still to
+// be formed by the loss), and s slots are free.  With r the least repetition count such that
+// β(s, r) >= n = t1 - t0, the state entering t0 + m is kept in a slot, where m takes the
+// largest value that leaves the right part n - m steps with s - 1 slots and r repetitions
+// (n - m <= β(s - 1, r)) and the left part m steps with s slots and r - 1 repetitions
+// (m <= β(s, r - 1)); since β(s, r) = β(s - 1, r) + β(s, r - 1), such m exists.  The right part is
+// reversed first, then the left one from `start`.  Without free slots, each state is recomputed
+// from `start`.
+struct AdjPlanner {
+  std::vector<AdjAction>& out;
+  int64_t T;
+  int64_t fwd = 0;
+  std::vector<bool> used;
+
+  // forward from the state entering t_from (at `from`) to the state entering t_to, the last step
+  // into `dst` (or a work buffer when dst is kLocWork), returning the location
+  int advance(int from, int64_t t_from, int64_t t_to, int dst) {
+    int cur = from;
+    for (int64_t t = t_from; t < t_to; ++t) {
+      int next;
+      if (t + 1 == t_to && dst != kLocWork) next = dst;
+      else next = (cur == kLocWork) ? kLocWork + 1 : kLocWork;  // the work buffer not read now
+      out.push_back({AdjAction::FWD, cur, next, t});
+      ++fwd;
+      cur = next;
+    }
+    return cur;
+  }
+  int take_slot() {
+    for (size_t j = 0; j < used.size(); ++j)
+      if (!used[j]) {
+        used[j] = true;
+        return (int)j;
+      }
+    return -100;  // not reached: the recursion never holds more slots than it was given
+  }
+  void adj(int64_t t, int src) { out.push_back({AdjAction::ADJ, src, 0, t}); }
+  void loss_from(int start, int64_t t_start) {  // B_{T-1} from the state entering t_start
+    const int loc = advance(start, t_start, T, kLocWork);
+    out.push_back({AdjAction::LOSS, loc, 0, T});
+  }
+  void reverse(int start, int64_t t0, int64_t t1, int64_t s, bool need_loss) {
+    const int64_t n = t1 - t0;
+    if (n == 1 || s == 0) {
+      if (need_loss) loss_from(start, t0);
+      for (int64_t t = t1 - 1; t >= t0; --t) adj(t, t == t0 ? start : advance(start, t0, t, kLocWork));
+      return;
+    }
+    int64_t r = 1;
+    while (binomial_beta(s, r) < n) ++r;
+    int64_t m = std::min<int64_t>(binomial_beta(s, r - 1), n - 1);
+    m = std::max<int64_t>(m, std::max<int64_t>(1, n - binomial_beta(s - 1, r)));
+    const int sl = take_slot();
+    advance(start, t0, t0 + m, sl);
+    reverse(sl, t0 + m, t1, s - 1, need_loss);
+    used[sl] = false;
+    reverse(start, t0, t0 + m, s, false);
+  }
+};
+
 int afail(lbm_adjoint* a, int status, const std::string& msg) {
   if (a) a->err = msg;
   drop_if_cuda(status);
@@ -1748,7 +1831,7 @@ const void* ctx_params(lbm_ctx* c) {
   return c->storage == LBM_STORE_F64 ? static_cast<const void*>(&c->pd) : static_cast<const void*>(&c->pf);
 }
 
-// The whole forward sweep, the checkpointed reverse sweep and the sensitivity sums.
+// The plan's forward steps, loss and reverse steps, then ∂L/∂u0 and the sensitivity sums.
 cudaError_t adjoint_sequence(lbm_adjoint* a) {
   lbm_ctx* c = a->ctx;
   cudaStream_t s = c->stream;
@@ -1760,58 +1843,32 @@ cudaError_t adjoint_sequence(lbm_adjoint* a) {
   const void* prm = ctx_params(c);
   double* loss_slots = a->d_slots;
   double* par_slots = a->d_slots + nb;
+  auto loc = [&](int l) -> void* {
+    if (l == kLocA0) return a->a0;
+    if (l == kLocWork || l == kLocWork + 1) return a->work[l - kLocWork];
+    return a->slot[(size_t)l];
+  };
   cudaError_t e = cudaMemsetAsync(a->d_slots, 0, (size_t)nb * (1 + kAdjParams) * sizeof(double), s);
   if (e != cudaSuccess) return e;
   // A_0
   e = adj_launch(0, c->qid, c->storage, c->coll, prm, args, nullptr, 0, nullptr, a->a0, nullptr, nb, a->d_u0, nullptr,
                  nullptr, s);
   if (e != cudaSuccess) return e;
-  // forward, keeping B_{ck-1} at every segment boundary
-  auto fwd_step = [&](const void* src, void* dst, bool first) {
-    OpArgs o = base_args(c, first ? OP_COLLIDE : OP_FUSED);
-    o.src = src;
-    o.dst = dst;
-    o.stream = s;
-    return kRun[c->qid](o);
-  };
-  for (int64_t t = 0; t < a->T; ++t) {
-    void* dst = a->fwd[t & 1];
-    e = fwd_step(t == 0 ? a->a0 : a->fwd[(t - 1) & 1], dst, t == 0);
+  for (const AdjAction& x : a->plan) {
+    if (x.kind == AdjAction::FWD) {  // B_t from the state entering step t (A_0 for t = 0: collision only)
+      OpArgs o = base_args(c, x.t == 0 ? OP_COLLIDE : OP_FUSED);
+      o.src = loc(x.src);
+      o.dst = loc(x.dst);
+      o.stream = s;
+      e = kRun[c->qid](o);
+    } else if (x.kind == AdjAction::LOSS) {  // loss and λ_T from A_T = S(B_{T-1})
+      e = adj_launch(1, c->qid, c->storage, c->coll, prm, args, loc(x.src), 1, nullptr, a->lam[a->T & 1], loss_slots,
+                     nb, nullptr, a->d_ut, nullptr, s);
+    } else {  // λ_t from λ_{t+1} and A_t (pulled from B_{t-1}, or A_0 read as it is)
+      e = adj_launch(2, c->qid, c->storage, c->coll, prm, args, loc(x.src), x.t == 0 ? 0 : 1, a->lam[(x.t + 1) & 1],
+                     a->lam[x.t & 1], par_slots, nb, nullptr, nullptr, nullptr, s);
+    }
     if (e != cudaSuccess) return e;
-    if ((t + 1) % a->k == 0 && t + 1 < a->T) {
-      e = cudaMemcpyAsync(a->ckpt[(t + 1) / a->k], dst, a->bytes, cudaMemcpyDeviceToDevice, s);
-      if (e != cudaSuccess) return e;
-    }
-  }
-  // loss and λ_T from A_T = S(B_{T-1})
-  e = adj_launch(1, c->qid, c->storage, c->coll, prm, args, a->fwd[(a->T - 1) & 1], 1, nullptr, a->lam[a->T & 1],
-                 loss_slots, nb, nullptr, a->d_ut, nullptr, s);
-  if (e != cudaSuccess) return e;
-  // reverse sweep, one segment at a time from the last
-  for (int64_t cc = a->nck - 1; cc >= 0; --cc) {
-    const int64_t t0 = cc * a->k;
-    const int64_t t1 = std::min<int64_t>((cc + 1) * a->k, a->T) - 1;
-    // recompute B_t for t0 <= t < t1 into seg[t - t0]
-    for (int64_t t = t0; t < t1; ++t) {
-      const void* src = (t == 0) ? a->a0 : (t == t0 ? a->ckpt[cc] : a->seg[t - 1 - t0]);
-      e = fwd_step(src, a->seg[t - t0], t == 0);
-      if (e != cudaSuccess) return e;
-    }
-    for (int64_t t = t1; t >= t0; --t) {
-      const void* src;
-      int pull = 1;
-      if (t == 0) {
-        src = a->a0;
-        pull = 0;
-      } else if (t == t0) {
-        src = a->ckpt[cc];
-      } else {
-        src = a->seg[t - 1 - t0];
-      }
-      e = adj_launch(2, c->qid, c->storage, c->coll, prm, args, src, pull, a->lam[(t + 1) & 1], a->lam[t & 1],
-                     par_slots, nb, nullptr, nullptr, nullptr, s);
-      if (e != cudaSuccess) return e;
-    }
   }
   e = adj_launch(3, c->qid, c->storage, c->coll, prm, args, nullptr, 0, a->lam[0], nullptr, nullptr, nb, a->d_u0,
                  nullptr, a->d_grad, s);
@@ -1825,27 +1882,36 @@ cudaError_t adjoint_sequence(lbm_adjoint* a) {
 
 extern "C" {
 
-int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_t checkpoint_every) {
-  if (!out || !c || nsteps < 1) return LBM_ERR_INVALID;
+int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_t slots) {
+  if (!out || !c || nsteps < 1 || slots < 0) return LBM_ERR_INVALID;
   *out = nullptr;
   if (c->qid != LBM_D2Q9 && c->qid != LBM_D2Q13) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: D2Q9 / D2Q13 only");
   if (c->coll != LBM_SRT && c->coll != LBM_TRT) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: SRT / TRT only");
   if (c->storage != LBM_STORE_F64 && c->storage != LBM_STORE_F32_DEV)
     return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: FP64 or FP32-deviation storage only");
-  if (c->pd.nbc != 0) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: periodic lattices only");
   if (c->force_kind != LBM_FORCE_NONE && c->force_kind != LBM_FORCE_CONSTANT)
     return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: uniform force only");
   DeviceGuard device_guard(c->device);
   lbm_adjoint* a = new lbm_adjoint();
   a->ctx = c;
   a->T = nsteps;
-  int64_t k = checkpoint_every > 0 ? checkpoint_every : (int64_t)std::ceil(std::sqrt((double)nsteps));
-  a->k = std::max<int64_t>(1, std::min<int64_t>(k, nsteps));
-  a->nck = (a->T + a->k - 1) / a->k;
+  // default: the fewest slots with which no step is recomputed more than twice
+  int64_t sl = slots;
+  if (sl == 0) {
+    sl = 1;
+    while (binomial_beta(sl, 2) < nsteps) ++sl;
+  }
+  a->nslots = std::min<int64_t>(sl, std::max<int64_t>(nsteps - 1, 0));
+  {
+    AdjPlanner pl{a->plan, a->T};
+    pl.used.assign((size_t)a->nslots, false);
+    pl.reverse(kLocA0, 0, a->T, a->nslots, true);
+    a->forward_steps = pl.fwd;
+  }
   a->bytes = (size_t)c->n * c->Q * c->elem;
   a->nblocks = (int)std::min<int64_t>((c->n + kAdjThreads - 1) / kAdjThreads, 152 * 4);
-  bool ok = dev_malloc(&a->a0, a->bytes) && dev_malloc(&a->fwd[0], a->bytes) &&
-            dev_malloc(&a->fwd[1], a->bytes) && dev_malloc(&a->lam[0], a->bytes) &&
+  bool ok = dev_malloc(&a->a0, a->bytes) && dev_malloc(&a->work[0], a->bytes) &&
+            dev_malloc(&a->work[1], a->bytes) && dev_malloc(&a->lam[0], a->bytes) &&
             dev_malloc(&a->lam[1], a->bytes) &&
             dev_malloc(&a->d_u0, (size_t)c->n * 2 * sizeof(double)) &&
             dev_malloc(&a->d_ut, (size_t)c->n * 2 * sizeof(double)) &&
@@ -1853,10 +1919,8 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
             dev_malloc(&a->d_slots, (size_t)a->nblocks * (1 + kAdjParams) * sizeof(double)) &&
             dev_malloc(&a->d_out, 8 * sizeof(double)) &&
             host_malloc(&a->h_out, 8 * sizeof(double));
-  a->ckpt.assign(a->nck, nullptr);
-  for (int64_t cc = 1; ok && cc < a->nck; ++cc) ok = dev_malloc(&a->ckpt[cc], a->bytes);
-  a->seg.assign(a->k, nullptr);
-  for (int64_t j = 0; ok && j < a->k; ++j) ok = dev_malloc(&a->seg[j], a->bytes);
+  a->slot.assign((size_t)a->nslots, nullptr);
+  for (int64_t j = 0; ok && j < a->nslots; ++j) ok = dev_malloc(&a->slot[(size_t)j], a->bytes);
   if (!ok) {
     lbm_adjoint_destroy(a);
     return fail(c, LBM_ERR_NOMEM, "adjoint: device memory for checkpoints");
@@ -1865,15 +1929,24 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
   return LBM_OK;
 }
 
+int32_t lbm_adjoint_info(const lbm_adjoint* a, int64_t* slots, int64_t* forward_steps, int64_t* device_bytes) {
+  if (!a) return LBM_ERR_INVALID;
+  if (slots) *slots = a->nslots;
+  if (forward_steps) *forward_steps = a->forward_steps;
+  if (device_bytes)  // states (A_0, two work buffers, the slots, two adjoint states) and the planes
+    *device_bytes = (int64_t)(a->bytes * (size_t)(5 + a->nslots) + (size_t)a->ctx->n * 6 * sizeof(double) +
+                              (size_t)a->nblocks * (1 + kAdjParams) * sizeof(double) + 8 * sizeof(double));
+  return LBM_OK;
+}
+
 void lbm_adjoint_destroy(lbm_adjoint* a) {
   if (!a) return;
   DeviceGuard device_guard(a->ctx->device);
   cudaStreamSynchronize(a->ctx->stream);
   if (a->graph) cudaGraphExecDestroy(a->graph);
-  void* bufs[] = {a->a0, a->fwd[0], a->fwd[1], a->lam[0], a->lam[1], a->d_u0, a->d_ut, a->d_grad, a->d_slots, a->d_out};
+  void* bufs[] = {a->a0, a->work[0], a->work[1], a->lam[0], a->lam[1], a->d_u0, a->d_ut, a->d_grad, a->d_slots, a->d_out};
   for (void* b : bufs) cudaFree(b);
-  for (void* b : a->ckpt) cudaFree(b);
-  for (void* b : a->seg) cudaFree(b);
+  for (void* b : a->slot) cudaFree(b);
   if (a->h_out) cudaFreeHost(a->h_out);
   delete a;
 }
@@ -1913,7 +1986,7 @@ int32_t lbm_adjoint_run(lbm_adjoint* a, const double* u0, const double* u_target
     a->graph_stream = s;
   }
   if (cudaGraphLaunch(a->graph, s) != cudaSuccess) return afail(a, LBM_ERR_CUDA, "adjoint: graph launch");
-  c->last_launches = 3 * a->T;
+  c->last_launches = (int64_t)a->plan.size() + 5;
   if (cudaMemcpyAsync(a->h_out, a->d_out, 6 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return afail(a, LBM_ERR_CUDA, "adjoint: result copy");
   if (grad_u0 && cudaMemcpyAsync(grad_u0, a->d_grad, vb, cudaMemcpyDefault, s) != cudaSuccess)

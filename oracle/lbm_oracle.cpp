@@ -853,11 +853,12 @@ static void stream(Model& m, const std::vector<double>& f, std::vector<double>& 
 }
 
 // apply!(bcs, q, f_new, f_old): boundary_conditions.jl:6-20 in list order;
-// BounceBack bounce_back.jl:8-72; MovingWall moving_wall.jl:17-38
-static void apply_bcs(Model& m, std::vector<double>& fnew, const std::vector<double>& fold) {
-  const Quad& q = m.q;
-  const int nx = m.nx, ny = m.ny;
-  for (const orc_bc& bc : m.bcs) {
+// BounceBack bounce_back.jl:8-72; MovingWall moving_wall.jl:17-38.  R is double, or the Dual of
+// the forward-mode derivative (orc_tangent_loss).
+template <class R>
+static void apply_bcs_t(const Quad& q, int nx, int ny, const std::vector<orc_bc>& bcs, R* fnew, const R* fold) {
+  auto idx = [&](int x, int y, int i) { return (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * i); };
+  for (const orc_bc& bc : bcs) {
     if (bc.kind == 0) {
       for (int i = 0; i < q.Q; ++i) {
         const int o = opposite(q, i);
@@ -865,15 +866,13 @@ static void apply_bcs(Model& m, std::vector<double>& fnew, const std::vector<dou
           for (int y = bc.y_lo; y <= bc.y_hi; ++y) {
             const bool skip = bc.direction == 0 ? (y + q.cy[o] <= ny) : (y + q.cy[o] > 0);
             if (skip) continue;
-            for (int x = bc.x_lo; x <= bc.x_hi; ++x)
-              fnew[m.idx(x - 1, y - 1, i)] = fold[m.idx(x - 1, y - 1, o)];
+            for (int x = bc.x_lo; x <= bc.x_hi; ++x) fnew[idx(x - 1, y - 1, i)] = fold[idx(x - 1, y - 1, o)];
           }
         } else {  // East / West
           for (int x = bc.x_lo; x <= bc.x_hi; ++x) {
             const bool skip = bc.direction == 1 ? (x + q.cx[o] <= nx) : (x + q.cx[o] > 0);
             if (skip) continue;
-            for (int y = bc.y_lo; y <= bc.y_hi; ++y)
-              fnew[m.idx(x - 1, y - 1, i)] = fold[m.idx(x - 1, y - 1, o)];
+            for (int y = bc.y_lo; y <= bc.y_hi; ++y) fnew[idx(x - 1, y - 1, i)] = fold[idx(x - 1, y - 1, o)];
           }
         }
       }
@@ -885,11 +884,14 @@ static void apply_bcs(Model& m, std::vector<double>& fnew, const std::vector<dou
         const int o = opposite(q, i);
         for (int y = 1; y <= ny; ++y) {
           if (y + q.cy[o] <= ny) continue;
-          for (int x = 1; x <= nx; ++x) fnew[m.idx(x - 1, y - 1, i)] = fold[m.idx(x - 1, y - 1, o)] + 2 * a1;
+          for (int x = 1; x <= nx; ++x) fnew[idx(x - 1, y - 1, i)] = fold[idx(x - 1, y - 1, o)] + R(2 * a1);
         }
       }
     }
   }
+}
+static void apply_bcs(Model& m, std::vector<double>& fnew, const std::vector<double>& fold) {
+  apply_bcs_t<double>(m.q, m.nx, m.ny, m.bcs, fnew.data(), fold.data());
 }
 
 }  // namespace orc
@@ -1469,8 +1471,9 @@ int orc_run(int qid, const orc_problem* p, const orc_collision* cm, int nbc, con
 // u0, ut, du0: arrays [2][ny][nx] (component, y, x).
 int orc_tangent_loss(int qid, int kind, const double* tau, const double* F, int nx, int ny, const double* u0,
                      const double* ut, const double* seed, const double* du0, long nsteps, int nthreads,
-                     double* out) {
-  if ((kind != 0 && kind != 1) || nx <= 0 || ny <= 0 || nsteps < 0) return -1;
+                     const orc_bc* bcs, int nbc, double* out) {
+  if ((kind != 0 && kind != 1) || nx <= 0 || ny <= 0 || nsteps < 0 || nbc < 0 || (nbc > 0 && !bcs)) return -1;
+  const std::vector<orc_bc> bclist(bcs, bcs + nbc);
   const Quad q = make_quad(qid);
   const int Q = q.Q;
   const size_t nn = (size_t)nx * ny, n = nn * Q;
@@ -1497,6 +1500,7 @@ int orc_tangent_loss(int qid, int kind, const double* tau, const double* F, int 
       }
     }
     stream_periodic(q, nx, ny, b.data(), a.data(), nthreads);
+    apply_bcs_t<Dual>(q, nx, ny, bclist, a.data(), b.data());
   }
   Dual L = 0.0;
   for (int y = 0; y < ny; ++y)

@@ -105,7 +105,7 @@ def lib():
         L.orc_run.argtypes = [C.c_int, C.POINTER(OrcProblem), C.POINTER(OrcCollision), C.c_int,
                               C.POINTER(OrcBC), C.c_long, C.c_long, C.c_double, C.c_int, dp]
         L.orc_tangent_loss.argtypes = [C.c_int, C.c_int, dp, dp, C.c_int, C.c_int, dp, dp, dp, C.c_void_p,
-                                       C.c_long, C.c_int, dp]
+                                       C.c_long, C.c_int, C.c_void_p, C.c_int, dp]
         L.orc_tangent_loss.restype = C.c_int
         L.orc_max_threads.restype = C.c_int
         _lib = L
@@ -381,12 +381,12 @@ def run(q, p, cm, bcs, f0, t_first, t_last, dt=0.0, nthreads=1):
     return f
 
 
-def tangent_loss(q, kind, taus, F, u0, ut, nsteps, seed=(0.0, 0.0, 0.0, 0.0), du0=None, nthreads=1):
-    """L = Σ |u(f_T) - ut|² after `nsteps` collide → periodic stream steps from
+def tangent_loss(q, kind, taus, F, u0, ut, nsteps, seed=(0.0, 0.0, 0.0, 0.0), du0=None, nthreads=1, bcs=()):
+    """L = Σ |u(f_T) - ut|² after `nsteps` collide → periodic stream → apply!(bcs) steps from
     f_0 = equilibrium(1, u0) (SRT `kind` "SRT" with τ = taus[0], TRT with τ_s, τ_a = taus, uniform
-    lattice force F), and its forward-mode derivative along seed = (dτ_0, dτ_1, dF_x, dF_y) and
-    the u0 direction du0, propagated with dual numbers.  u0, ut, du0: shape (2, ny, nx).
-    Returns (L, dL)."""
+    lattice force F, the boundary conditions `bcs` built by bc()), and its forward-mode derivative
+    along seed = (dτ_0, dτ_1, dF_x, dF_y) and the u0 direction du0, propagated with dual numbers.
+    u0, ut, du0: shape (2, ny, nx).  Returns (L, dL)."""
     u0 = np.ascontiguousarray(u0, dtype=np.float64)
     ut = np.ascontiguousarray(ut, dtype=np.float64)
     _, ny, nx = u0.shape
@@ -397,9 +397,11 @@ def tangent_loss(q, kind, taus, F, u0, ut, nsteps, seed=(0.0, 0.0, 0.0, 0.0), du
         assert d.shape == u0.shape
     t = np.array([float(taus[0]), float(taus[1] if len(taus) > 1 else taus[0])])
     out = np.zeros(2)
+    arr = (OrcBC * max(1, len(bcs)))(*bcs)
     rc = lib().orc_tangent_loss(qid(q), {"SRT": 0, "TRT": 1}[kind], t, np.array(F, dtype=np.float64), nx, ny,
                                 u0, ut, np.array(seed, dtype=np.float64),
-                                d.ctypes.data if d is not None else None, int(nsteps), int(nthreads), out)
+                                d.ctypes.data if d is not None else None, int(nsteps), int(nthreads),
+                                C.cast(arr, C.c_void_p) if len(bcs) else None, len(bcs), out)
     if rc != 0:
         raise ValueError(f"orc_tangent_loss: status {rc}")
     return float(out[0]), float(out[1])

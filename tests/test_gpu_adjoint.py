@@ -9,11 +9,11 @@ NX = NY = 32
 STEPS = 120
 
 
-def _setup(lbm, storage="f64", nsteps=STEPS, tau_s=0.8, F=(2e-6, -1e-6), ck=0):
+def _setup(lbm, storage="f64", nsteps=STEPS, tau_s=0.8, F=(2e-6, -1e-6), slots=0, bcs=()):
     q = lbm.D2Q9()
     tau_a = lbm.trt_magic(tau_s)
     return lbm.AdjointProblem(q, NX, NY, lbm.TRT.fields(tau_s, tau_a), force=F, nsteps=nsteps,
-                              checkpoint_every=ck, storage=storage)
+                              slots=slots, storage=storage, boundary_conditions=bcs)
 
 
 def _fields(lbm):
@@ -124,18 +124,31 @@ def test_adjoint_matches_oracle_forward_mode(lbm_gpu, O, kind):
         assert ad == pytest.approx(fm, rel=1e-8), (ad, fm)
 
 
-def test_checkpoint_interval_does_not_change_gradients(lbm_gpu):
+@pytest.mark.parametrize("walls", [False, True])
+def test_checkpoint_slots_do_not_change_gradients(lbm_gpu, walls):
+    """Binomial checkpointing with 1, 2, 5, the default and T - 1 slots: the same forward states are
+    recomputed, so loss and gradients are bitwise the same; fewer slots cost more forward steps, and
+    with s slots no step is recomputed more than r times, C(s + r, s) >= T."""
     lbm = lbm_gpu
     u0, ut = _fields(lbm)
-    outs = []
-    for ck in (1, 7, 0, STEPS):
-        prob = _setup(lbm, ck=ck)
+    bcs = _walls(lbm) if walls else ()
+    outs, infos = [], []
+    for sl in (1, 2, 5, 0, STEPS - 1):
+        prob = _setup(lbm, slots=sl, bcs=bcs)
         outs.append(prob.run(u0, ut))
+        infos.append(prob.info())
         prob.close()
     for o in outs[1:]:
         assert o["loss"] == outs[0]["loss"]
         np.testing.assert_array_equal(o["grad_u0"], outs[0]["grad_u0"])
         assert o["dtau_s"] == outs[0]["dtau_s"]
+    from math import comb
+    for info in infos:
+        s = info["slots"]
+        r = next(r for r in range(1, STEPS + 1) if comb(s + r, s) >= STEPS)
+        assert STEPS <= info["forward_steps"] <= (r + 1) * STEPS, info
+    assert infos[-1]["forward_steps"] < infos[0]["forward_steps"]
+    assert infos[-1]["device_bytes"] > infos[0]["device_bytes"]
 
 
 def test_fp32_adjoint_close_to_fp64(lbm_gpu):
@@ -210,3 +223,76 @@ def test_other_sets_and_srt_match_finite_differences(lbm_gpu, qname, coll):
     fd_fx = fd(lambda e: loss(tau, (F[0] + e, F[1])), 1e-7)
     assert res["dtau_s"] == pytest.approx(fd_tau, rel=1e-6, abs=1e-12)
     assert res["dF"][0] == pytest.approx(fd_fx, rel=1e-6, abs=1e-12)
+
+
+def _walls(lbm, nx=NX, ny=NY, lid=False):
+    if lid:
+        return [lbm.BounceBack(lbm.East(), (1, nx), (1, ny)), lbm.BounceBack(lbm.South(), (1, nx), (1, ny)),
+                lbm.BounceBack(lbm.West(), (1, nx), (1, ny)), lbm.MovingWall(lbm.North(), (1, nx), (1, ny), (0.01, 0.0))]
+    return [lbm.BounceBack(lbm.North(), (1, nx), (1, ny)), lbm.BounceBack(lbm.South(), (1, nx), (1, ny))]
+
+
+def _owalls(O, nx=NX, ny=NY, lid=False):
+    if lid:
+        return [O.bc("bounce_back", "east", (1, nx), (1, ny)), O.bc("bounce_back", "south", (1, nx), (1, ny)),
+                O.bc("bounce_back", "west", (1, nx), (1, ny)),
+                O.bc("moving_wall", "north", (1, nx), (1, ny), u=(0.01, 0.0))]
+    return [O.bc("bounce_back", "north", (1, nx), (1, ny)), O.bc("bounce_back", "south", (1, nx), (1, ny))]
+
+
+def test_walled_channel_adjoint_matches_finite_differences(lbm_gpu):
+    """The 32 x 32 TRT channel with bounce-back walls North and South and a body force (the
+    benchmark channel's boundaries, bounce_back.jl:8-72): ∂L/∂τ_s, ∂L/∂τ_a, ∂L/∂F_x and a
+    directional ∂L/∂u0 against fourth-order central differences of the device forward model."""
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    tau_s, F = 0.8, (2e-6, 0.0)
+    tau_a = lbm.trt_magic(tau_s)
+    bcs = _walls(lbm)
+    prob = _setup(lbm, tau_s=tau_s, F=F, bcs=bcs, slots=6)
+    res = prob.run(u0, ut)
+    prob.close()
+
+    def loss(ts, ta, Fx, u):
+        p = lbm.AdjointProblem(lbm.D2Q9(), NX, NY, lbm.TRT.fields(ts, ta), force=(Fx, 0.0), nsteps=STEPS,
+                               boundary_conditions=_walls(lbm))
+        L = p.loss(u, ut)
+        p.close()
+        return L
+
+    def fd(fun, h):
+        return (fun(-2 * h) - 8 * fun(-h) + 8 * fun(h) - fun(2 * h)) / (12 * h)
+
+    v = np.random.default_rng(17).normal(size=u0.shape)
+    checks = [(res["dtau_s"], fd(lambda e: loss(tau_s + e, tau_a, F[0], u0), 1e-4)),
+              (res["dtau_a"], fd(lambda e: loss(tau_s, tau_a + e, F[0], u0), 1e-4)),
+              (res["dF"][0], fd(lambda e: loss(tau_s, tau_a, F[0] + e, u0), 1e-7)),
+              (float(np.sum(res["grad_u0"] * v)), fd(lambda e: loss(tau_s, tau_a, F[0], u0 + e * v), 1e-5))]
+    for ad, ref in checks:
+        assert abs(ad - ref) <= 1e-6 * max(abs(ref), 1e-12), (ad, ref)
+
+
+@pytest.mark.parametrize("lid", [False, True])
+def test_walled_adjoint_matches_oracle_forward_mode(lbm_gpu, O, lid):
+    """Walled channel, and a lid-driven cavity (bounce-back East, South, West, moving lid North):
+    the adjoint's derivatives against the forward-mode (dual-number) derivatives of the oracle's
+    collide -> stream -> apply! loop with the same boundary list (≤ 1e-8)."""
+    lbm = lbm_gpu
+    u0, ut = _fields(lbm)
+    tau_s, F = 0.8, (2e-6, 0.0)
+    tau_a = lbm.trt_magic(tau_s)
+    prob = _setup(lbm, tau_s=tau_s, F=F, bcs=_walls(lbm, lid=lid), slots=4)
+    res = prob.run(u0, ut)
+    prob.close()
+    v = np.random.default_rng(19).normal(size=u0.shape)
+    obcs = _owalls(O, lid=lid)
+
+    def tangent(seed, du0=None):
+        return O.tangent_loss("D2Q9", "TRT", (tau_s, tau_a), F, u0, ut, STEPS, seed=seed, du0=du0, bcs=obcs)
+
+    L, d_ts = tangent((1, 0, 0, 0))
+    assert res["loss"] == pytest.approx(L, rel=1e-10)
+    for ad, fm in [(res["dtau_s"], d_ts), (res["dtau_a"], tangent((0, 1, 0, 0))[1]),
+                   (res["dF"][0], tangent((0, 0, 1, 0))[1]),
+                   (float(np.sum(res["grad_u0"] * v)), tangent((0, 0, 0, 0), v)[1])]:
+        assert ad == pytest.approx(fm, rel=1e-8), (ad, fm)
