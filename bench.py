@@ -478,9 +478,11 @@ def main():
     ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev", "f32sr"])
     ap.add_argument("--profile", action="store_true",
                     help="time only the device loop of the chosen storage (for profiler runs)")
-    ap.add_argument("--case", default="poiseuille", choices=["poiseuille", "mrt_d2q37", "trt_sweep", "adjoint"],
+    ap.add_argument("--case", default="poiseuille",
+                    choices=["poiseuille", "mrt_d2q37", "trt_sweep", "adjoint", "shear_wave_study"],
                     help="with --profile: the workload run (D2Q9 TRT Poiseuille 4096^2, D2Q37 regularised MRT "
-                         "shear wave 2048^2, the batched TRT sweep, or the D2Q9 TRT 512^2 adjoint)")
+                         "shear wave 2048^2, the batched TRT sweep, the D2Q9 TRT 512^2 adjoint, or the batched "
+                         "shear-wave convergence study)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other configurations (Taylor-Green 64^2, D2Q37 MRT, batched study, adjoint)")
     args = ap.parse_args()
@@ -516,6 +518,17 @@ def main():
         res = lbm.run_trt_sweep(pts, scale=1, torch=torch)
         res.pop("rows")
         print(json.dumps({"case": "trt_sweep", **res}))
+        return 0
+    if args.profile and args.case == "shear_wave_study":  # the 28 runs batched, once
+        models, times, _ = lbm.build_shear_wave_study_models(("D2Q4", "D2Q5", "D2Q9", "D2Q13", "D2Q17", "D2Q21",
+                                                              "D2Q37"))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lbm.simulate_batch(models, times)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": "shear_wave_study", "seconds": time.perf_counter() - t0}))
+        for m in models:
+            m.close()
         return 0
     if args.profile and args.case == "adjoint":
         print(json.dumps({"case": "adjoint", **bench_adjoint(torch, lbm, steps=args.steps)}))
