@@ -1,0 +1,6 @@
+// Kernel instantiations for the D2Q21 velocity set with F32DevSR storage.
+#include "lbm_ops.cuh"
+
+namespace lbm {
+cudaError_t run_op_q21_f32sr(const OpArgs& a) { return run_op_s<D2Q21, F32DevSR>(a, *a.px); }
+}  // namespace lbm

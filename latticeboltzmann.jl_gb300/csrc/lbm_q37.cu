@@ -7,6 +7,7 @@ cudaError_t run_op_q37_f64(const OpArgs& a);
 cudaError_t run_op_q37_df64(const OpArgs& a);
 cudaError_t run_op_q37_f32(const OpArgs& a);
 cudaError_t run_op_q37_f16(const OpArgs& a);
+cudaError_t run_op_q37_f32sr(const OpArgs& a);
 
 cudaError_t run_op_q37(const OpArgs& a) {
   switch (a.storage) {
@@ -14,6 +15,7 @@ cudaError_t run_op_q37(const OpArgs& a) {
     case LBM_STORE_DF64_DEV: return run_op_q37_df64(a);
     case LBM_STORE_F32_DEV: return run_op_q37_f32(a);
     case LBM_STORE_F16_DEV: return run_op_q37_f16(a);
+    case LBM_STORE_F32_DEV_SR: return run_op_q37_f32sr(a);
     default: return cudaErrorInvalidValue;
   }
 }
