@@ -116,11 +116,12 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_model(lbm, storage, tau_s):
+def build_model(lbm, storage, tau_s, n=None):
     q = lbm.D2Q9()
     nu = (tau_s - 0.5) / q.speed_of_sound_squared
     u_max = 0.05
-    problem = lbm.PoiseuilleFlow.fields(1.0, u_max, nu, NX, NY, 1.0, (1.0, 1.0), 1.0)
+    nx = ny = n or NX
+    problem = lbm.PoiseuilleFlow.fields(1.0, u_max, nu, nx, ny, 1.0, (1.0, 1.0), 1.0)
     problem.G = 1e-6 / (u_max * problem.delta_t() * problem.viscosity())  # lattice force 1e-6
     cm = lbm.TRT.fields(tau_s, 0.5 + 0.25 / (tau_s - 0.5), "problem")
     f0 = lbm.initialize(lbm.ZeroVelocityInitialCondition(), q, problem)
@@ -483,6 +484,8 @@ def main():
                     help="with --profile: the workload run (D2Q9 TRT Poiseuille 4096^2, D2Q37 regularised MRT "
                          "shear wave 2048^2, the batched TRT sweep, the D2Q9 TRT 512^2 adjoint, or the batched "
                          "shear-wave convergence study)")
+    ap.add_argument("--n", type=int, default=0,
+                    help="with --profile and the Poiseuille case: an n x n channel instead of 4096 x 4096")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other configurations (Taylor-Green 64^2, D2Q37 MRT, batched study, adjoint)")
     args = ap.parse_args()
@@ -529,6 +532,13 @@ def main():
         print(json.dumps({"case": "shear_wave_study", "seconds": time.perf_counter() - t0}))
         for m in models:
             m.close()
+        return 0
+    if args.profile and args.n:  # a smaller channel of the same kind, for profiler captures
+        problem, model, _ = build_model(lbm, args.storage, tau_s, args.n)
+        sec, launches = time_device(torch, model, args.steps, args.warmup, problem.delta_t())
+        model.close()
+        print(json.dumps({"case": "poiseuille", "n": args.n, "storage": args.storage,
+                          "mlups": args.n * args.n * args.steps / sec / 1e6, "launches": launches}))
         return 0
     if args.profile and args.case == "adjoint":
         print(json.dumps({"case": "adjoint", **bench_adjoint(torch, lbm, steps=args.steps)}))

@@ -292,7 +292,7 @@ struct F32DevSR {
   }
 };
 
-// 24 uniform bits from (node, population, step): the three are mixed by odd multipliers and the
+// 32 uniform bits from (node, population, step): the three are mixed by odd multipliers and the
 // result goes through the "lowbias32" integer finaliser (xor-shift / multiply rounds with the
 // constants C. Wellons published for it).  Counter-based, so a run is reproducible.
 __device__ __forceinline__ unsigned sr_bits(unsigned node, unsigned pop, unsigned step) {
@@ -302,18 +302,20 @@ __device__ __forceinline__ unsigned sr_bits(unsigned node, unsigned pop, unsigne
   h ^= h >> 15;
   h *= 0x846CA68Bu;
   h ^= h >> 16;
-  return h >> 8;
+  return h;
 }
 
 // Stochastic rounding of a normalised float-float value (|lo| at most half an ulp of hi) to a
-// float, with the 24 uniform bits u: the neighbour n of hi towards lo is taken when
-// u 2^-24 |n - hi| < |lo|.  |n - hi| is a power of two, so the comparison is exact.
-__device__ __forceinline__ float round_stochastic(float hi, float lo, unsigned u) {
+// float, with the uniform bits h: the neighbour n of hi towards lo is taken when u |n - hi| < |lo|,
+// u in [0, 1) the top 23 bits of h (formed from the bits, as 1.f..2.f minus one: no integer-to-float
+// conversion).  |n - hi| is a power of two, so the product and the comparison are exact.
+__device__ __forceinline__ float round_stochastic(float hi, float lo, unsigned h) {
   if (lo == 0.f || hi == 0.f || !isfinite(hi)) return __fadd_rn(hi, lo);
   const int b = __float_as_int(hi);
   const float n = __int_as_float(b + (((lo > 0.f) == (hi > 0.f)) ? 1 : -1));
   const float gap = fabsf(__fsub_rn(n, hi));
-  return __fmul_rn(__fmul_rn((float)u, gap), 0x1p-24f) < fabsf(lo) ? n : hi;
+  const float u = __fsub_rn(__int_as_float(0x3F800000u | (h >> 9)), 1.0f);
+  return __fmul_rn(u, gap) < fabsf(lo) ? n : hi;
 }
 
 // ---------------------------------------------------------------------------------------
