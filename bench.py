@@ -33,7 +33,8 @@ NX = NY = 4096
 Q = 9
 SEED = 20240611
 METRIC = "D2Q9 TRT 4096² MLUPS & %HBM peak: FP64 vs FP32-dev, batched, adjoint"
-BYTES_PER_LU = {"f64": 2 * Q * 8, "df64dev": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2, "f32sr": 2 * Q * 4}
+BYTES_PER_LU = {"f64": 2 * Q * 8, "df64dev": 2 * Q * 8, "f32dev": 2 * Q * 4, "f16dev": 2 * Q * 2, "f32sr": 2 * Q * 4,
+                "f64dd": 2 * Q * 8}
 ACCURACY_STEPS = 2000  # the configuration's run length, over which each storage's error is measured
 
 
@@ -476,7 +477,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev", "f32sr"])
+    ap.add_argument("--storage", default="f64", choices=["f64", "df64dev", "f32dev", "f16dev", "f32sr", "f64dd"])
     ap.add_argument("--profile", action="store_true",
                     help="time only the device loop of the chosen storage (for profiler runs)")
     ap.add_argument("--case", default="poiseuille",
@@ -582,13 +583,13 @@ def main():
         # accuracy over the configuration's 2000 steps (untimed): every storage's velocity column
         # against the FP64 run's
         ux_acc = {}
-        for st in ("f64", "df64dev", "f32dev", "f16dev", "f32sr"):
+        for st in ("f64", "df64dev", "f32dev", "f16dev", "f32sr", "f64dd"):
             _, mx, _ = build_model(lbm, st, tau_s)
             mx.lattice.step(ACCURACY_STEPS, 0, dt)
             ux_acc[st] = mx.lattice.macroscopic()[1]
             mx.close()
         ref_acc = ux_acc["f64"][:, 0]
-        for st in ("df64dev", "f32dev", "f16dev", "f32sr"):
+        for st in ("df64dev", "f32dev", "f16dev", "f32sr", "f64dd"):
             _, mx, _ = build_model(lbm, st, tau_s)
             sx, _ = time_device(torch, mx, args.steps, args.warmup, dt)
             ux = mx.lattice.macroscopic()[1][:, 0]
@@ -602,6 +603,9 @@ def main():
                          "error_measure": "max over the lattice of |ux - ux_f64| / max |ux_f64|"}
         extra["f32sr"]["arithmetic"] = ("FP32 deviation storage, float-float arithmetic, collision outputs stored "
                                         "with stochastic rounding")
+        extra["f64dd"]["arithmetic"] = ("FP64 storage (the f64 bytes and values), float-float arithmetic on g = f - w; "
+                                        "the FP64 pipe forms g on load and w + g on store")
+        extra["f64dd"]["dtype"] = "f64-storage, float-float arithmetic"
     if rank == 0 and not args.profile and not args.no_extras and args.storage == "f64":
         extra["configs"] = {"tgv64": bench_tgv64(torch, lbm), "mrt_d2q37": bench_mrt_d2q37(torch, lbm),
                             "batched": bench_batched(torch, lbm), "trt_sweep": bench_trt_sweep(torch, lbm),

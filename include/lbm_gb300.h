@@ -77,13 +77,16 @@ typedef enum { LBM_SRT = 0, LBM_TRT = 1, LBM_MRT = 2, LBM_ITERATIVE_INIT = 3 } l
  *             output stored with stochastic rounding (unbiased; a counter-based hash of node,
  *             population and time index draws the rounding, so runs are reproducible): the
  *             rounding of a small, steady increment (a body force) no longer accumulates.
- *             Single lattices only (batches and the adjoint refuse it). */
+ *             Single lattices only (batches and the adjoint refuse it).
+ *   F64_DD    f in FP64 (the F64 bytes and values), float-float arithmetic on g = f - w: the FP64
+ *             pipe only forms g on load and w + g on store.  Single lattices only. */
 typedef enum {
   LBM_STORE_F64 = 0,
   LBM_STORE_F32_DEV = 1,
   LBM_STORE_F16_DEV = 2,
   LBM_STORE_DF64_DEV = 3,
-  LBM_STORE_F32_DEV_SR = 4
+  LBM_STORE_F32_DEV_SR = 4,
+  LBM_STORE_F64_DD = 5
 } lbm_storage;
 
 /* Forcing, applied as the reference does: a velocity shift of the equilibrium, u + τ F

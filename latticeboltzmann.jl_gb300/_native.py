@@ -19,9 +19,9 @@ LBM_OK, LBM_ERR_INVALID, LBM_ERR_CUDA, LBM_ERR_NOMEM, LBM_ERR_UNSUPPORTED, LBM_E
 
 QUAD_IDS = {"D2Q4": 0, "D2Q5": 1, "D2Q9": 2, "D2Q13": 3, "D2Q17": 4, "D2Q21": 5, "D2Q37": 6}
 SRT, TRT, MRT, ITERATIVE_INIT = 0, 1, 2, 3
-STORE_F64, STORE_F32_DEV, STORE_F16_DEV, STORE_DF64_DEV, STORE_F32_DEV_SR = 0, 1, 2, 3, 4
+STORE_F64, STORE_F32_DEV, STORE_F16_DEV, STORE_DF64_DEV, STORE_F32_DEV_SR, STORE_F64_DD = 0, 1, 2, 3, 4, 5
 STORAGE_IDS = {"f64": STORE_F64, "f32dev": STORE_F32_DEV, "f16dev": STORE_F16_DEV, "df64dev": STORE_DF64_DEV,
-               "f32sr": STORE_F32_DEV_SR}
+               "f32sr": STORE_F32_DEV_SR, "f64dd": STORE_F64_DD}
 FORCE_NONE, FORCE_CONSTANT, FORCE_FIELD, FORCE_SHEAR = 0, 1, 2, 3
 BOUNCE_BACK, MOVING_WALL = 0, 1
 NORTH, EAST, SOUTH, WEST = 0, 1, 2, 3

@@ -378,7 +378,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   if (d->nx < 1 || d->ny < 1 || d->nx >= (int64_t(1) << 31) || d->ny >= (int64_t(1) << 31) ||
       d->nx * d->ny >= (int64_t(1) << 31))
     return LBM_ERR_INVALID;
-  if (d->storage < 0 || d->storage > 4) return LBM_ERR_INVALID;
+  if (d->storage < 0 || d->storage > 5) return LBM_ERR_INVALID;
   if (d->collision < 0 || d->collision > 3) return LBM_ERR_INVALID;
   if (d->force_kind < 0 || d->force_kind > 3) return LBM_ERR_INVALID;
   if (d->nbc < 0 || d->nbc > LBM_MAX_BC || (d->nbc > 0 && !d->bcs)) return LBM_ERR_INVALID;
@@ -398,7 +398,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   c->nx = d->nx;
   c->ny = d->ny;
   c->n = d->nx * d->ny;
-  c->elem = (d->storage == LBM_STORE_F64 || d->storage == LBM_STORE_DF64_DEV) ? 8
+  c->elem = (d->storage == LBM_STORE_F64 || d->storage == LBM_STORE_DF64_DEV || d->storage == LBM_STORE_F64_DD) ? 8
             : (d->storage == LBM_STORE_F32_DEV || d->storage == LBM_STORE_F32_DEV_SR) ? 4 : 2;
 
   for (int b = 0; b < d->nbc; ++b) {
@@ -437,6 +437,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
     p.dym[s + 3] = (int)(((s % d->ny) + d->ny) % d->ny);
   }
   for (int i = 0; i < LBM_MAX_Q; ++i) p.w[i] = i < c->Q ? d->weights[i] : 0.0;
+  for (int i = 0; i < LBM_MAX_Q; ++i) p.wf[i] = p.w[i];
   p.cs = d->speed_of_sound_squared;
   const double* tau = d->tau;
   if (c->coll == LBM_SRT || c->coll == LBM_ITERATIVE_INIT) {
@@ -505,6 +506,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
     q.dym[k] = p.dym[k];
   }
   for (int i = 0; i < LBM_MAX_Q; ++i) q.w[i] = (float)p.w[i];
+  for (int i = 0; i < LBM_MAX_Q; ++i) q.wf[i] = p.w[i];
   q.cs = (float)p.cs;
   q.om_a = (float)p.om_a;
   q.om_b = (float)p.om_b;
@@ -587,6 +589,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
     x.dym[k] = p.dym[k];
   }
   for (int i = 0; i < LBM_MAX_Q; ++i) x.w[i] = dd(p.w[i]);
+  for (int i = 0; i < LBM_MAX_Q; ++i) x.wf[i] = p.w[i];
   for (int i = 0; i < LBM_MAX_Q; ++i) x.w1[i] = dd(p.w1[i]);
   x.cs = dd(p.cs);
   x.om_a = dd(p.om_a);
@@ -667,7 +670,8 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
         drop_reported_error();
         return LBM_ERR_NOMEM;
       }
-    } else if (c->storage == LBM_STORE_DF64_DEV || c->storage == LBM_STORE_F32_DEV_SR) {  // float-float arithmetic
+    } else if (c->storage == LBM_STORE_DF64_DEV || c->storage == LBM_STORE_F32_DEV_SR ||
+               c->storage == LBM_STORE_F64_DD) {  // float-float arithmetic
       std::vector<dd> tmp(cnt);
       for (size_t k = 0; k < cnt; ++k) tmp[k] = dd(d->nonlinear[k]);
       if (!dev_malloc(&c->d_nonlinear, cnt * sizeof(dd)) ||
@@ -1159,7 +1163,8 @@ int32_t lbm_batch_create(lbm_batch** out, lbm_ctx* const* members, int32_t count
     const lbm_ctx* c = members[k];
     if (!c || c->device != c0->device || c->storage != c0->storage || c->coll != c0->coll) return LBM_ERR_INVALID;
     if (c->coll == LBM_ITERATIVE_INIT) return LBM_ERR_UNSUPPORTED;
-    if (c->storage == LBM_STORE_F16_DEV || c->storage == LBM_STORE_F32_DEV_SR) return LBM_ERR_UNSUPPORTED;
+    if (c->storage == LBM_STORE_F16_DEV || c->storage == LBM_STORE_F32_DEV_SR || c->storage == LBM_STORE_F64_DD)
+      return LBM_ERR_UNSUPPORTED;
   }
   {  // a context may appear once: the batch advances each member's own buffers
     std::vector<lbm_ctx*> sorted(members, members + count);

@@ -212,7 +212,8 @@ struct F64 {
   using T = double;     // element in HBM
   using C = double;     // compute type
   static constexpr bool DEV = false;
-  static constexpr bool SR = false;  // collision outputs stored with stochastic rounding
+  static constexpr bool SR = false;    // collision outputs stored with stochastic rounding
+  static constexpr bool WIDE = false;  // stores f but computes on g = f - w (F64DD)
   static constexpr int id = LBM_STORE_F64;
   __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
@@ -223,6 +224,7 @@ struct F32Dev {
   using C = float;
   static constexpr bool DEV = true;
   static constexpr bool SR = false;
+  static constexpr bool WIDE = false;
   static constexpr int id = LBM_STORE_F32_DEV;
   __device__ __forceinline__ static C ld(const T* p) { return __ldg(p); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = v; }
@@ -238,6 +240,7 @@ struct F16Dev {
   using C = float;
   static constexpr bool DEV = true;
   static constexpr bool SR = false;
+  static constexpr bool WIDE = false;
   static constexpr int id = LBM_STORE_F16_DEV;
   __device__ __forceinline__ static C ld(const T* p) { return __half2float(__ldg(p)); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = __float2half_rn(v); }
@@ -255,6 +258,7 @@ struct DF64Dev {
   using C = dd;
   static constexpr bool DEV = true;
   static constexpr bool SR = false;
+  static constexpr bool WIDE = false;
   static constexpr int id = LBM_STORE_DF64_DEV;
   __device__ __forceinline__ static C ld(const T* p) {
     const float2 v = __ldg(p);
@@ -282,6 +286,7 @@ struct F32DevSR {
   using C = dd;
   static constexpr bool DEV = true;
   static constexpr bool SR = true;
+  static constexpr bool WIDE = false;
   static constexpr int id = LBM_STORE_F32_DEV_SR;
   __device__ __forceinline__ static C ld(const T* p) { return dd(__ldg(p), 0.f); }
   __device__ __forceinline__ static void st(T* p, C v) { *p = __fadd_rn(v.hi, v.lo); }
@@ -317,6 +322,52 @@ __device__ __forceinline__ float round_stochastic(float hi, float lo, unsigned h
   const float u = __fsub_rn(__int_as_float(0x3F800000u | (h >> 9)), 1.0f);
   return __fmul_rn(u, gap) < fabsf(lo) ? n : hi;
 }
+
+// FP64 storage (f itself, the reference's bytes) with float-float arithmetic on the deviation
+// g = f - w.  On this GPU a double <-> float conversion instruction runs at the FP64 rate, as slow as
+// the FP64 arithmetic it would replace, so the splits are made with integer operations: a load
+// forms g = f - w with one FP64 subtraction and splits it into a float-float pair from its bits; a
+// store rebuilds the doubles of hi and lo from their bits and forms w + (hi + lo) with two FP64
+// additions (hi + lo is exact in FP64 when lo lies within 29 bits of hi, as the collision's
+// normalised outputs do, and rounds once otherwise).  The collision is the float-float one of
+// DF64Dev, so a value carries 48 bits on the deviation, below FP64's own rounding of f.
+struct F64DD {
+  using T = double;
+  using C = dd;
+  static constexpr bool DEV = true;
+  static constexpr bool SR = false;
+  static constexpr bool WIDE = true;
+  static constexpr int id = LBM_STORE_F64_DD;
+  // x as hi + lo: hi the top 24 significand bits of x (truncated), lo the next 29 rounded to a float,
+  // renormalised; doubles outside 2^-74 .. 2^100 take the conversion instructions
+  __device__ __forceinline__ static dd split(double x) {
+    const long long b = __double_as_longlong(x);
+    if ((b & 0x7FFFFFFFFFFFFFFFll) == 0) return dd(0.f, 0.f);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e >= 949 && e <= 1023 + 100) {
+      const unsigned long long m = (unsigned long long)b & 0xFFFFFFFFFFFFFull;
+      const unsigned sgn = (unsigned)((unsigned long long)b >> 63) << 31;
+      const float hi = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(m >> 29));
+      const float scale = __uint_as_float((unsigned)(e - 1023 - 52 + 127) << 23);
+      const float lo = __uint_as_float(__float_as_uint(__fmul_rn(__uint2float_rn((unsigned)(m & 0x1FFFFFFFull)), scale)) | sgn);
+      return fast_two_sum(hi, lo);
+    }
+    const float h = __double2float_rn(x);
+    return dd(h, __double2float_rn(x - (double)h));
+  }
+  // the double of a float from its bits (normal floats and zero; others take the conversion)
+  __device__ __forceinline__ static double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)f;
+    return __longlong_as_double(((long long)(u >> 31) << 63) | ((long long)(e - 127u + 1023u) << 52) |
+                                ((long long)(u & 0x7FFFFFu) << 29));
+  }
+  __device__ __forceinline__ static C from_f(double f, double w) { return split(__dsub_rn(f, w)); }
+  __device__ __forceinline__ static double to_f(C g, double w) {
+    return __dadd_rn(w, __dadd_rn(widen(g.hi), widen(g.lo)));
+  }
+};
 
 // ---------------------------------------------------------------------------------------
 // Kernel parameter blocks (passed by value; they live in the constant bank).
@@ -358,6 +409,7 @@ struct StepParams {
   int time_step;               // time (t0 + time_step) Δt (steps of a CUDA graph, see step_time)
   long long step_index;        // time index of this step when time_base is not set (the counter of
                                // stochastic rounding, step_counter)
+  double wf[LBM_MAX_Q];        // the weights in FP64 (F64DD: f = w + g on load and store)
   const CT* nonlinear;         // ITER: nonlinear equilibrium term planes (device)
   int nbc;
   BCDev bc[LBM_MAX_BC];

@@ -158,6 +158,7 @@ cudaError_t run_op(const OpArgs& a) {
     case LBM_STORE_F16_DEV: return run_op_s<L, F16Dev>(a, *a.pf);
     case LBM_STORE_DF64_DEV: return run_op_s<L, DF64Dev>(a, *a.px);
     case LBM_STORE_F32_DEV_SR: return run_op_s<L, F32DevSR>(a, *a.px);
+    case LBM_STORE_F64_DD: return run_op_s<L, F64DD>(a, *a.px);
     default: return cudaErrorInvalidValue;
   }
 }

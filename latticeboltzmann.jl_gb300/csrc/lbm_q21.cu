@@ -8,6 +8,7 @@ cudaError_t run_op_q21_df64(const OpArgs& a);
 cudaError_t run_op_q21_f32(const OpArgs& a);
 cudaError_t run_op_q21_f16(const OpArgs& a);
 cudaError_t run_op_q21_f32sr(const OpArgs& a);
+cudaError_t run_op_q21_f64dd(const OpArgs& a);
 
 cudaError_t run_op_q21(const OpArgs& a) {
   switch (a.storage) {
@@ -16,6 +17,7 @@ cudaError_t run_op_q21(const OpArgs& a) {
     case LBM_STORE_F32_DEV: return run_op_q21_f32(a);
     case LBM_STORE_F16_DEV: return run_op_q21_f16(a);
     case LBM_STORE_F32_DEV_SR: return run_op_q21_f32sr(a);
+    case LBM_STORE_F64_DD: return run_op_q21_f64dd(a);
     default: return cudaErrorInvalidValue;
   }
 }

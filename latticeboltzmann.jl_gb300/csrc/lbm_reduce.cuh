@@ -266,7 +266,8 @@ __global__ void __launch_bounds__(kBlockX) narrow_kernel(StepParams<typename S::
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
       const double f = in[(size_t)i * p.n + k];
-      S::st(dst + (size_t)i * p.n + k, (typename S::C)(S::DEV ? f - r.w[i] : f));
+      if constexpr (S::WIDE) dst[(size_t)i * p.n + k] = f;  // f itself, exactly
+      else S::st(dst + (size_t)i * p.n + k, (typename S::C)(S::DEV ? f - r.w[i] : f));
     }
   }
 }
@@ -380,7 +381,8 @@ __global__ void __launch_bounds__(kBlockX) init_fields_kernel(StepParams<typenam
                           (cv[0] * cv[1]) * in.sxy[k] + (cv[1] * cv[1] - css) * in.syy[k];
         f = f + (in.coef * (in.times_rho ? rho : 1.0)) * r.w[i] * HS;
       }
-      S::st(dst + (size_t)i * p.n + k, (typename S::C)(S::DEV ? f - r.w[i] : f));
+      if constexpr (S::WIDE) dst[(size_t)i * p.n + k] = f;  // f itself, exactly
+      else S::st(dst + (size_t)i * p.n + k, (typename S::C)(S::DEV ? f - r.w[i] : f));
     });
   }
 }

@@ -26,6 +26,20 @@ __device__ __forceinline__ size_t plane_off(const StepParams<CT>& p, int i) {
   return (size_t)(unsigned)p.n * (unsigned)i;
 }
 
+// Population i at `ptr` in the compute type, and its store: S::ld / S::st, except for a storage
+// that keeps f itself but computes on the deviation (F64DD), which forms g = f - w on load and
+// w + g on store with the FP64 weight.
+template <class S, class CT>
+__device__ __forceinline__ typename S::C load_pop(const StepParams<CT>& p, const typename S::T* ptr, int i) {
+  if constexpr (S::WIDE) return S::from_f(__ldg(ptr), p.wf[i]);
+  else return S::ld(ptr);
+}
+template <class S, class CT>
+__device__ __forceinline__ void store_pop(const StepParams<CT>& p, typename S::T* ptr, int i, typename S::C v) {
+  if constexpr (S::WIDE) *ptr = S::to_f(v, p.wf[i]);
+  else S::st(ptr, v);
+}
+
 // Periodic pull offsets: xw[k] = (x - (k - R)) mod nx, yo[k] = ((y - (k - R)) mod ny) * nx.
 template <class L, class CT>
 __device__ __forceinline__ void pull_offsets(const StepParams<CT>& p, int x, int y, int* xw, int* yo) {
@@ -52,7 +66,7 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) {
     const int idx = yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)];
-    f[i] = S::ld(src + plane_off(p, i) + idx);
+    f[i] = load_pop<S>(p, src + plane_off(p, i) + idx, i);
   }
   if (p.nbc > 0 &&
       (y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R)) {
@@ -70,13 +84,13 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
           else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
           else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
           else hit = x1 + L::cx(o) <= 0;
-          if (hit) f[i] = S::ld(src + plane_off(p, o) + node);
+          if (hit) f[i] = load_pop<S>(p, src + plane_off(p, o) + node, o);
         }
       } else {  // MovingWall{North}: whole top wall, ignores xs / ys
 #pragma unroll
         for (int i = 0; i < L::Q; ++i) {
           const int o = L::opp(i);
-          if (y1 + L::cy(o) > p.ny) f[i] = S::ld(src + plane_off(p, o) + node) + (typename S::C)bc.add[i];
+          if (y1 + L::cy(o) > p.ny) f[i] = load_pop<S>(p, src + plane_off(p, o) + node, o) + (typename S::C)bc.add[i];
         }
       }
     }
@@ -88,7 +102,7 @@ __device__ __forceinline__ void load_streamed(const StepParams<CT>& p, const typ
 template <class L, class S, class CT>
 __device__ __forceinline__ typename S::C pop_streamed(const StepParams<CT>& p, const typename S::T* __restrict__ src,
                                                       int x, int y, const int* xw, const int* yo, bool near, int i) {
-  typename S::C v = S::ld(src + plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
+  typename S::C v = load_pop<S>(p, src + plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)], i);
   if (near) {
     const int node = y * p.nx + x;
     const int y1 = y + 1, x1 = x + 1;
@@ -102,9 +116,9 @@ __device__ __forceinline__ typename S::C pop_streamed(const StepParams<CT>& p, c
         else if (bc.dir == LBM_SOUTH) hit = y1 + L::cy(o) <= 0;
         else if (bc.dir == LBM_EAST) hit = x1 + L::cx(o) > p.nx;
         else hit = x1 + L::cx(o) <= 0;
-        if (hit) v = S::ld(src + plane_off(p, o) + node);
+        if (hit) v = load_pop<S>(p, src + plane_off(p, o) + node, o);
       } else if (y1 + L::cy(o) > p.ny) {
-        v = S::ld(src + plane_off(p, o) + node) + (typename S::C)bc.add[i];
+        v = load_pop<S>(p, src + plane_off(p, o) + node, o) + (typename S::C)bc.add[i];
       }
     }
   }
@@ -115,7 +129,7 @@ template <class L, class S, class CT>
 __device__ __forceinline__ void load_local(const StepParams<CT>& p, const typename S::T* __restrict__ src,
                                            int node, typename S::C* f) {
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) f[i] = S::ld(src + plane_off(p, i) + node);
+  for (int i = 0; i < L::Q; ++i) f[i] = load_pop<S>(p, src + plane_off(p, i) + node, i);
 }
 
 // Physical time of the step: p.time, or, for the steps of a captured CUDA graph of a lattice with a
@@ -140,7 +154,7 @@ template <class S, class CT>
 __device__ __forceinline__ void store_out(const StepParams<CT>& p, typename S::T* dst, int i, int node,
                                           typename S::C v) {
   if constexpr (S::SR) dst[plane_off(p, i) + node] = round_stochastic(v.hi, v.lo, sr_bits(node, i, step_counter(p)));
-  else S::st(dst + plane_off(p, i) + node, v);
+  else store_pop<S>(p, dst + plane_off(p, i) + node, i, v);
 }
 
 // Lattice force at node (x, y), lattice_force(problem, x, y, t) (problems.jl:103-104).  `time()`
@@ -692,7 +706,10 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
       auto out = [&](int i, CT val) { store_out<S>(p, dst, i, node, val); };
       if constexpr (MODE == 0) {
         mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
-                            [&](auto I) { return S::ld(src + plane_off(p, decltype(I)::value) + node); }, out);
+                            [&](auto I) {
+                              constexpr int i = decltype(I)::value;
+                              return load_pop<S>(p, src + plane_off(p, i) + node, i);
+                            }, out);
       } else {
         int xw[2 * L::R + 1], yo[2 * L::R + 1];
         pull_offsets<L>(p, x, y, xw, yo);
@@ -704,7 +721,7 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
         } else {
           mrt_node<L, S::DEV>(p, sFx, sFy, has_force, [&](auto I) {
             constexpr int i = decltype(I)::value;
-            return S::ld(src + plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]);
+            return load_pop<S>(p, src + plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)], i);
           }, out);
         }
       }
@@ -718,7 +735,7 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
         for (int i = 0; i < L::Q; ++i) store_out<S>(p, dst, i, node, v[i]);
       } else {
 #pragma unroll
-        for (int i = 0; i < L::Q; ++i) S::st(dst + plane_off(p, i) + node, v[i]);
+        for (int i = 0; i < L::Q; ++i) store_pop<S>(p, dst + plane_off(p, i) + node, i, v[i]);
       }
     }
   }
@@ -756,7 +773,8 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
       static_for<0, L::Q>([&](auto I) {
         constexpr int i = decltype(I)::value;
         const T* a = src + plane_off(p, i) + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
-        if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
+        if constexpr (S::WIDE) v[i] = pack2(load_pop<S>(p, a, i), load_pop<S>(p, a + 1, i));
+        else if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
         else v[i] = pack2(S::ld(a), S::ld(a + 1));
       });
     } else {
@@ -783,6 +801,9 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
         const float a = round_stochastic(v[i].hi.lo(), v[i].lo.lo(), sr_bits(node, i, step));
         const float b = round_stochastic(v[i].hi.hi(), v[i].lo.hi(), sr_bits(node + 1, i, step));
         *reinterpret_cast<unsigned long long*>(dst + plane_off(p, i) + node) = pf2(a, b).r;
+      } else if constexpr (S::WIDE) {  // both lanes as one aligned 16-byte store
+        *reinterpret_cast<double2*>(dst + plane_off(p, i) + node) =
+            make_double2(S::to_f(dd(v[i].hi.lo(), v[i].lo.lo()), p.wf[i]), S::to_f(dd(v[i].hi.hi(), v[i].lo.hi()), p.wf[i]));
       } else {
         S::st2(dst + plane_off(p, i) + node, v[i]);
       }

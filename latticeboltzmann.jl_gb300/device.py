@@ -29,7 +29,8 @@ class DeviceLattice:
     force: None | ("constant", (Fx, Fy)) | ("field", array (2, NY, NX)) |
            ("shear", [c0..c5], x_coords, y_coords)
     storage: "f64" | "df64dev" (float-float deviation) | "f32dev" | "f16dev" | "f32sr" (FP32 deviation,
-             float-float arithmetic, stochastically rounded stores)
+             float-float arithmetic, stochastically rounded stores) | "f64dd" (FP64 storage, float-float
+             arithmetic on the deviation)
     nonlinear: the (Q, NY, NX) term of the iterative-initialisation collision model
     """
 

@@ -44,8 +44,9 @@ class LatticeBoltzmannModel:
     """LatticeBoltzmannModel(problem, q; collision_model=SRT, initialization_strategy, process_method)
     with the populations resident on the GPU.  `storage` selects FP64 ("f64"), the float-float
     deviation storage ("df64dev", FP64-class, FP32 pipes), the FP32 / FP16 deviation storage
-    ("f32dev" / "f16dev"), or the FP32 deviation storage with float-float arithmetic and
-    stochastically rounded stores ("f32sr").  Closed-form initial conditions are built on the
+    ("f32dev" / "f16dev"), the FP32 deviation storage with float-float arithmetic and
+    stochastically rounded stores ("f32sr"), or FP64 storage with float-float arithmetic on the
+    deviation ("f64dd").  Closed-form initial conditions are built on the
     device from their macroscopic planes unless `device_init` is False or `f0` (shape (Q, NY, NX))
     is given."""
 

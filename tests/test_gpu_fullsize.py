@@ -7,9 +7,9 @@ run length).
 
   - D2Q9 TRT (magic Λ = 1/4) Poiseuille channel 4096 x 4096, bounce-back North / South,
     constant lattice force 1e-6, τ_s drawn from U[0.55, 1.5] with the benchmark's seed, u = 0
-    start, 2000 steps, FP64 and float-float storage.
+    start, 2000 steps, FP64, float-float and FP64-with-float-float-arithmetic storage.
   - D2Q37 regularised MRT shear wave 2048 x 2048, u_x = 0.01 sin(2π y / Ny), τ = 0.6,
-    equilibrium start, 500 steps, FP64 and float-float storage."""
+    equilibrium start, 500 steps, the same three storages."""
 import numpy as np
 import pytest
 
@@ -75,7 +75,7 @@ def _oracle_shear_wave(O, ny, steps, tau):
     return _ORACLE[key]
 
 
-@pytest.mark.parametrize("storage", ["f64", "df64dev"])
+@pytest.mark.parametrize("storage", ["f64", "df64dev", "f64dd"])
 def test_channel_4096_2000_steps_matches_oracle(lbm_gpu, O, storage):
     lbm = lbm_gpu
     n, steps, tau_s = 4096, 2000, _tau_s()
@@ -92,7 +92,7 @@ def test_channel_4096_2000_steps_matches_oracle(lbm_gpu, O, storage):
     assert err <= TOL, err
 
 
-@pytest.mark.parametrize("storage", ["f64", "df64dev"])
+@pytest.mark.parametrize("storage", ["f64", "df64dev", "f64dd"])
 def test_mrt_d2q37_shear_wave_2048_500_steps_matches_oracle(lbm_gpu, O, storage):
     lbm = lbm_gpu
     n, steps, tau = 2048, 500, 0.6

@@ -1,4 +1,4 @@
-"""CUDA path (liblbm_gb300 through its C ABI) against the CPU oracle, FP64 storage.
+"""CUDA path (liblbm_gb300 through its C ABI) against the CPU oracle, FP64-class storages.
 
 The fused pull kernel is compared with the oracle's collide! -> stream! -> apply! loop on
 the same inputs after N steps, for every velocity set, the SRT / TRT / regularised-MRT
@@ -52,7 +52,9 @@ def _run_pair(lbm, O, qname, nx, ny, coll, taus, steps, bcs_spec=(), force=None,
     return f_gpu, f_ref
 
 
-STORAGES = ["f64", "df64dev"]  # the FP64-class storages: both held to the 1e-12 bound
+# the FP64-class storages, all held to the 1e-12 bound: FP64, the float-float deviation, and FP64
+# storage with float-float arithmetic on the deviation
+STORAGES = ["f64", "df64dev", "f64dd"]
 
 
 @pytest.mark.parametrize("storage", STORAGES)
