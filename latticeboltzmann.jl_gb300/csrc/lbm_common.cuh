@@ -360,8 +360,9 @@ struct F64DD {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xFFu;
     if (e == 0u || e == 0xFFu) return (double)f;
-    return __longlong_as_double(((long long)(u >> 31) << 63) | ((long long)(e - 127u + 1023u) << 52) |
-                                ((long long)(u & 0x7FFFFFu) << 29));
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                            ((unsigned long long)(e - 127u + 1023u) << 52) |
+                                            ((unsigned long long)(u & 0x7FFFFFu) << 29)));
   }
   __device__ __forceinline__ static C from_f(double f, double w) { return split(__dsub_rn(f, w)); }
   __device__ __forceinline__ static double to_f(C g, double w) {
