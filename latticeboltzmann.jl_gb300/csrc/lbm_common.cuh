@@ -339,7 +339,8 @@ struct F64DD {
   static constexpr bool WIDE = true;
   static constexpr int id = LBM_STORE_F64_DD;
   // x as hi + lo: hi the top 24 significand bits of x (truncated), lo the next 29 rounded to a float,
-  // renormalised; doubles outside 2^-74 .. 2^100 take the conversion instructions
+  // renormalised; doubles outside 2^-74 .. 2^100 take the conversion instructions.  The biased float
+  // exponent of lo, nb - 1 + e - 948, is at least 1 for e >= 949.
   __device__ __forceinline__ static dd split(double x) {
     const long long b = __double_as_longlong(x);
     if ((b & 0x7FFFFFFFFFFFFFFFll) == 0) return dd(0.f, 0.f);
@@ -348,8 +349,25 @@ struct F64DD {
       const unsigned long long m = (unsigned long long)b & 0xFFFFFFFFFFFFFull;
       const unsigned sgn = (unsigned)((unsigned long long)b >> 63) << 31;
       const float hi = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(m >> 29));
-      const float scale = __uint_as_float((unsigned)(e - 1023 - 52 + 127) << 23);
-      const float lo = __uint_as_float(__float_as_uint(__fmul_rn(__uint2float_rn((unsigned)(m & 0x1FFFFFFFull)), scale)) | sgn);
+      // lo = r 2^(e - 1075) for the 29 bits r below hi's, rounded to 24 bits (half away from zero)
+      // and assembled from its bits: an integer-to-float conversion also runs at the FP64 rate
+      const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+      float lo = 0.f;
+      if (r != 0u) {
+        int nb = 32 - __clz((int)r);  // significant bits of r, 1 .. 29
+        unsigned mant;
+        if (nb <= 24) {
+          mant = r << (24 - nb);
+        } else {
+          const int sh = nb - 24;
+          mant = (r + (1u << (sh - 1))) >> sh;
+          if (mant >> 24) {  // the rounding carried into a 25th bit
+            mant >>= 1;
+            ++nb;
+          }
+        }
+        lo = __uint_as_float(sgn | ((unsigned)(nb - 1 + e - 1075 + 127) << 23) | (mant & 0x7FFFFFu));
+      }
       return fast_two_sum(hi, lo);
     }
     const float h = __double2float_rn(x);

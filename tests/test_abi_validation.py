@@ -46,7 +46,7 @@ def test_status_strings_and_version(lbm, L):
 
 
 @pytest.mark.parametrize("field,value", [("quadrature", 7), ("quadrature", -1), ("nx", 0), ("ny", -3),
-                                         ("storage", 5), ("collision", 4), ("force_kind", 4)])
+                                         ("storage", 6), ("collision", 4), ("force_kind", 4)])
 def test_create_rejects_bad_descriptor_fields(lbm, L, field, value):
     assert _create(L, _desc(lbm, **{field: value})) == lbm._native.LBM_ERR_INVALID
 
