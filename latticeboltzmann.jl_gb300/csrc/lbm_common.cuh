@@ -339,19 +339,20 @@ struct F64DD {
   static constexpr bool WIDE = true;
   static constexpr int id = LBM_STORE_F64_DD;
   // x as hi + lo: hi the top 24 significand bits of x (truncated), lo the next 29 rounded to a float,
-  // renormalised; doubles outside 2^-74 .. 2^100 take the conversion instructions.  The biased float
-  // exponent of lo, nb - 1 + e - 948, is at least 1 for e >= 949.
+  // renormalised; doubles outside 2^-74 .. 2^100 take the conversion instructions.  Every bit
+  // operation is on the two 32-bit words of x (64-bit integer operations also issue to the FP64
+  // pipe on this GPU).  The biased float exponent of lo, nb - 1 + e - 948, is at least 1 for
+  // e >= 949.
   __device__ __forceinline__ static dd split(double x) {
-    const long long b = __double_as_longlong(x);
-    if ((b & 0x7FFFFFFFFFFFFFFFll) == 0) return dd(0.f, 0.f);
-    const int e = (int)((b >> 52) & 0x7FF);
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    if (((hw & 0x7FFFFFFFu) | lw) == 0u) return dd(0.f, 0.f);
+    const int e = (int)((hw >> 20) & 0x7FFu);
     if (e >= 949 && e <= 1023 + 100) {
-      const unsigned long long m = (unsigned long long)b & 0xFFFFFFFFFFFFFull;
-      const unsigned sgn = (unsigned)((unsigned long long)b >> 63) << 31;
-      const float hi = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(m >> 29));
+      const unsigned sgn = hw & 0x80000000u;
+      const float hi = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
       // lo = r 2^(e - 1075) for the 29 bits r below hi's, rounded to 24 bits (half away from zero)
       // and assembled from its bits: an integer-to-float conversion also runs at the FP64 rate
-      const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+      const unsigned r = lw & 0x1FFFFFFFu;
       float lo = 0.f;
       if (r != 0u) {
         int nb = 32 - __clz((int)r);  // significant bits of r, 1 .. 29
@@ -373,14 +374,15 @@ struct F64DD {
     const float h = __double2float_rn(x);
     return dd(h, __double2float_rn(x - (double)h));
   }
-  // the double of a float from its bits (normal floats and zero; others take the conversion)
+  // the double of a float from its bits, assembled as two 32-bit words (normal floats and zero;
+  // others take the conversion)
   __device__ __forceinline__ static double widen(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xFFu;
+    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
     if (e == 0u || e == 0xFFu) return (double)f;
-    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
-                                            ((unsigned long long)(e - 127u + 1023u) << 52) |
-                                            ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+    return __hiloint2double((int)((u & 0x80000000u) | ((e - 127u + 1023u) << 20) | ((u & 0x7FFFFFu) >> 3)),
+                            (int)((u & 7u) << 29));
   }
   __device__ __forceinline__ static C from_f(double f, double w) { return split(__dsub_rn(f, w)); }
   __device__ __forceinline__ static double to_f(C g, double w) {
