@@ -338,51 +338,44 @@ struct F64DD {
   static constexpr bool SR = false;
   static constexpr bool WIDE = true;
   static constexpr int id = LBM_STORE_F64_DD;
-  // x as hi + lo: hi the top 24 significand bits of x (truncated), lo the next 29 rounded to a float,
-  // renormalised; doubles outside 2^-74 .. 2^100 take the conversion instructions.  Every bit
-  // operation is on the two 32-bit words of x (64-bit integer operations also issue to the FP64
-  // pipe on this GPU).  The biased float exponent of lo, nb - 1 + e - 948, is at least 1 for
-  // e >= 949.
+  // x as hi + lo: hi the top 24 significand bits of x (truncated), lo the next 29 rounded to the
+  // nearest float, renormalised.  Integer and FP32 instructions only, with no branch to a
+  // conversion: on this GPU a double-float conversion, an integer-to-float conversion and a 64-bit
+  // integer operation all issue to the FP64 pipe, where even a predicated-off instruction takes
+  // its slot.  Every bit operation is on the two 32-bit words of x.  Range: |x| >= 2^-74 splits
+  // exactly as stated; for 2^-126 <= |x| < 2^-74 lo is flushed to zero (absolute error below
+  // 2^-98); smaller |x| (double subnormals and zero) give a signed zero; |x| >= 2^128 gives an
+  // infinity and a NaN stays a NaN.
   __device__ __forceinline__ static dd split(double x) {
     const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
-    if (((hw & 0x7FFFFFFFu) | lw) == 0u) return dd(0.f, 0.f);
     const int e = (int)((hw >> 20) & 0x7FFu);
-    if (e >= 949 && e <= 1023 + 100) {
-      const unsigned sgn = hw & 0x80000000u;
-      const float hi = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
-      // lo = r 2^(e - 1075) for the 29 bits r below hi's, rounded to 24 bits (half away from zero)
-      // and assembled from its bits: an integer-to-float conversion also runs at the FP64 rate
-      const unsigned r = lw & 0x1FFFFFFFu;
-      float lo = 0.f;
-      if (r != 0u) {
-        int nb = 32 - __clz((int)r);  // significant bits of r, 1 .. 29
-        unsigned mant;
-        if (nb <= 24) {
-          mant = r << (24 - nb);
-        } else {
-          const int sh = nb - 24;
-          mant = (r + (1u << (sh - 1))) >> sh;
-          if (mant >> 24) {  // the rounding carried into a 25th bit
-            mant >>= 1;
-            ++nb;
-          }
-        }
-        lo = __uint_as_float(sgn | ((unsigned)(nb - 1 + e - 1075 + 127) << 23) | (mant & 0x7FFFFFu));
-      }
-      return fast_two_sum(hi, lo);
-    }
-    const float h = __double2float_rn(x);
-    return dd(h, __double2float_rn(x - (double)h));
+    const unsigned sgn = hw & 0x80000000u;
+    const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+    // lo = r 2^(e - 1075) for the 29 bits r below hi's: r's top 23 and low 6 bits become exact
+    // floats through the 2^23 exponent trick, one FMA joins them (rounding to 24 bits) and the
+    // power-of-two scale places them; the scale is zero (lo flushed) for e < 949
+    const unsigned r = lw & 0x1FFFFFFFu;
+    const float ra = __fsub_rn(__uint_as_float(0x4B000000u | (r >> 6)), 8388608.f);
+    const float rb = __fsub_rn(__uint_as_float(0x4B000000u | (r & 63u)), 8388608.f);
+    const float scale = __uint_as_float((unsigned)max(e - 948, 0) << 23);
+    const float lo = __uint_as_float(__float_as_uint(__fmul_rn(__fmaf_rn(ra, 64.f, rb), scale)) | sgn);
+    const dd out = fast_two_sum(hi, lo);
+    const bool nan = e == 2047 && ((hw & 0xFFFFFu) | lw) != 0u;
+    const unsigned special = e < 897 ? sgn : (nan ? 0x7FC00000u : (sgn | 0x7F800000u));
+    const bool normal = e >= 897 && e <= 1150;
+    return dd(normal ? out.hi : __uint_as_float(special), normal ? out.lo : 0.f);
   }
-  // the double of a float from its bits, assembled as two 32-bit words (normal floats and zero;
-  // others take the conversion)
+  // the double of a float, assembled from its bits as two 32-bit words (normal, subnormal, zero,
+  // infinity and NaN alike; no conversion instruction)
   __device__ __forceinline__ static double widen(float f) {
     const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xFFu;
-    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (e == 0u || e == 0xFFu) return (double)f;
-    return __hiloint2double((int)((u & 0x80000000u) | ((e - 127u + 1023u) << 20) | ((u & 0x7FFFFFu) >> 3)),
-                            (int)((u & 7u) << 29));
+    const unsigned e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    // a float subnormal m 2^-149 is normalised: m << sh has its leading bit at position 23
+    const int sh = __clz((int)m) - 8;
+    const unsigned ms = (m << sh) & 0x7FFFFFu;
+    const unsigned E = e == 0u ? (m == 0u ? 0u : (unsigned)(897 - sh)) : (e == 0xFFu ? 0x7FFu : e + 896u);
+    const unsigned M = e == 0u ? ms : m;
+    return __hiloint2double((int)((u & 0x80000000u) | (E << 20) | (M >> 3)), (int)(M << 29));
   }
   __device__ __forceinline__ static C from_f(double f, double w) { return split(__dsub_rn(f, w)); }
   __device__ __forceinline__ static double to_f(C g, double w) {
