@@ -365,21 +365,47 @@ struct F64DD {
     const bool normal = e >= 897 && e <= 1150;
     return dd(normal ? out.hi : __uint_as_float(special), normal ? out.lo : 0.f);
   }
-  // the double of a float, assembled from its bits as two 32-bit words (normal, subnormal, zero,
-  // infinity and NaN alike; no conversion instruction)
-  __device__ __forceinline__ static double widen(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
-    // a float subnormal m 2^-149 is normalised: m << sh has its leading bit at position 23
-    const int sh = __clz((int)m) - 8;
-    const unsigned ms = (m << sh) & 0x7FFFFFu;
-    const unsigned E = e == 0u ? (m == 0u ? 0u : (unsigned)(897 - sh)) : (e == 0xFFu ? 0x7FFu : e + 896u);
-    const unsigned M = e == 0u ? ms : m;
-    return __hiloint2double((int)((u & 0x80000000u) | (E << 20) | (M >> 3)), (int)(M << 29));
+  // the double of a normalised pair hi + lo (|lo| <= ulp(hi) / 2, as every float-float addition
+  // leaves it), assembled from the bits: hi's significand times 2^29 plus lo's significand aligned
+  // to the same units, lo rounded half away from zero where its last bits fall below them (error
+  // at most 2^-52 |hi + lo|).  A zero or float-subnormal hi gives a signed zero and a
+  // float-subnormal lo is dropped (absolute error below 2^-126 either way); an infinite or NaN hi
+  // stays one.
+  __device__ __forceinline__ static double widen2(float h, float l) {
+    const unsigned uh = __float_as_uint(h), ul = __float_as_uint(l);
+    const int eh = (int)((uh >> 23) & 0xFFu), el = (int)((ul >> 23) & 0xFFu);
+    const unsigned mh = (uh & 0x7FFFFFu) | 0x800000u, ml = (ul & 0x7FFFFFu) | 0x800000u;
+    // L = lo / 2^(eh - 179) rounded, < 2^29: d = eh - el >= 24 for a normalised pair
+    const int d = eh - el;
+    const int sr = min(max(d - 29, 1), 31);
+    const unsigned down_l = d <= 29 ? (ml << (29 - d)) : ((ml + (1u << (sr - 1))) >> sr);
+    const unsigned L = (el == 0 || d > 53) ? 0u : down_l;
+    const unsigned a_hi = mh >> 3, a_lo = mh << 29;
+    unsigned r_hi, r_lo;
+    if (((uh ^ ul) & 0x80000000u) == 0u) {
+      r_hi = a_hi;
+      r_lo = a_lo | L;
+    } else {
+      r_hi = a_hi - (L > a_lo ? 1u : 0u);
+      r_lo = a_lo - L;
+    }
+    // a subtraction from a power-of-two hi can borrow the leading bit: shift it back into place
+    const unsigned dn = r_hi < 0x100000u ? 1u : 0u;
+    r_hi = dn ? ((r_hi << 1) | (r_lo >> 31)) : r_hi;
+    r_lo = r_lo << dn;
+    const unsigned sgn = uh & 0x80000000u;
+    const unsigned word = eh == 0 ? sgn
+                        : (eh == 255 ? (sgn | 0x7FF00000u | ((uh & 0x7FFFFFu) ? 0x80000u : 0u))
+                                     : (sgn | ((unsigned)(eh + 896 - (int)dn) << 20) | (r_hi & 0xFFFFFu)));
+    const unsigned lword = (eh == 0 || eh == 255) ? 0u : r_lo;
+    return __hiloint2double((int)word, (int)lword);
   }
   __device__ __forceinline__ static C from_f(double f, double w) { return split(__dsub_rn(f, w)); }
+  // collision outputs may be unnormalised pairs (a product's (p, e), |e| well below |p|): one
+  // fast two-sum normalises them for widen2
   __device__ __forceinline__ static double to_f(C g, double w) {
-    return __dadd_rn(w, __dadd_rn(widen(g.hi), widen(g.lo)));
+    const dd n = fast_two_sum(g.hi, g.lo);
+    return __dadd_rn(w, widen2(n.hi, n.lo));
   }
 };
 
