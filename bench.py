@@ -486,7 +486,7 @@ def main():
                          "shear wave 2048^2, the batched TRT sweep, the D2Q9 TRT 512^2 adjoint, or the batched "
                          "shear-wave convergence study)")
     ap.add_argument("--n", type=int, default=0,
-                    help="with --profile and the Poiseuille case: an n x n channel instead of 4096 x 4096")
+                    help="with --profile: an n x n lattice for the Poiseuille case (default 4096) and the D2Q37 MRT case (default 2048)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other configurations (Taylor-Green 64^2, D2Q37 MRT, batched study, adjoint)")
     args = ap.parse_args()
@@ -508,7 +508,7 @@ def main():
 
     if args.profile and args.case == "mrt_d2q37":
         q = lbm.D2Q37()
-        n = 2048
+        n = args.n or 2048
         problem = lbm.ShearWave(n, n, (0.6 - 0.5) / q.speed_of_sound_squared, 0.01)
         f0 = lbm.initialize(lbm.AnalyticalEquilibrium(), q, problem)
         m = lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.MRT(q, 0.6), storage=args.storage, f0=f0)
