@@ -379,12 +379,13 @@ def bench_adjoint(torch, lbm, n=512, steps=4000):
                    "forward_steps": info["forward_steps"], "device_bytes": info["device_bytes"],
                    "state_bytes": n * n * 9 * 4}
     # a memory budget: 8 slots instead of the default (every step recomputed at most r times,
-    # C(8 + r, 8) >= T), and the walled channel (bounce-back North / South)
-    for label, kw in (("f32dev_8_slots", {"slots": 8}),
-                      ("f32dev_channel_walls", {"boundary_conditions": [lbm.BounceBack(lbm.North(), (1, n), (1, n)),
-                                                                        lbm.BounceBack(lbm.South(), (1, n), (1, n))]})):
-        prob = lbm.AdjointProblem(q, n, n, lbm.TRT.fields(tau_s, lbm.trt_magic(tau_s)), force=(1e-6, 0.0),
-                                  nsteps=steps, storage="f32dev", **kw)
+    # C(8 + r, 8) >= T), the walled channel (bounce-back North / South), and the regularised MRT
+    trt = lbm.TRT.fields(tau_s, lbm.trt_magic(tau_s))
+    walls = [lbm.BounceBack(lbm.North(), (1, n), (1, n)), lbm.BounceBack(lbm.South(), (1, n), (1, n))]
+    for label, cm, kw in (("f32dev_8_slots", trt, {"slots": 8}),
+                          ("f32dev_channel_walls", trt, {"boundary_conditions": walls}),
+                          ("f32dev_mrt", lbm.MRT(q, tau_s), {})):
+        prob = lbm.AdjointProblem(q, n, n, cm, force=(1e-6, 0.0), nsteps=steps, storage="f32dev", **kw)
         prob.run(u0, ut, want_grad_u0=False)
         torch.cuda.synchronize()
         t0 = time.perf_counter()

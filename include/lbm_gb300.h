@@ -299,12 +299,14 @@ int32_t lbm_batch_share_stream(lbm_batch* batch);
 
 /* ---- adjoint (reverse-mode gradients) -----------------------------------------------------
  * No differentiation exists in the reference; this is the discrete adjoint of the fused step
- * for D2Q9 / D2Q13 lattices with SRT or TRT, a uniform force and the context's boundary
+ * for D2Q9 / D2Q13 lattices with SRT, TRT or regularised MRT, a uniform force and the context's boundary
  * conditions (bounce-back on any side, moving wall: the pull's transpose swaps opposite
  * populations at the walls), FP64 or FP32-deviation storage.  For the loss
  *   L = Σ_x |u(f_T) - u*|²,  f_0 = f_eq(ρ = 1, u0),  f_{t+1} = apply!(stream(collide(f_t))),  T = nsteps,
- * lbm_adjoint_run returns result[0] = L, result[1] = ∂L/∂τ_s (SRT: dL/dτ), result[2] = ∂L/∂τ_a
- * (TRT; 0 for SRT), result[3..4] = ∂L/∂F, and, if grad_u0 is not NULL, ∂L/∂u0 as two planes of
+ * lbm_adjoint_run returns result[0] = L, result[1] = ∂L/∂τ_s (SRT: dL/dτ; MRT: dL/dτ_2, the
+ * second-order relaxation time, which also scales the force shift, mrt.jl:91-95; the only one a
+ * second-order set's output depends on), result[2] = ∂L/∂τ_a (TRT; 0 for SRT and MRT),
+ * result[3..4] = ∂L/∂F, and, if grad_u0 is not NULL, ∂L/∂u0 as two planes of
  * nx*ny (Julia layout, like u0 and u_target).  Memory is bounded by binomial checkpointing
  * (Griewank's schedule): `slots` lattice states are kept (0 selects the fewest with which no
  * forward step is recomputed more than twice), and the reverse sweep recomputes the states it

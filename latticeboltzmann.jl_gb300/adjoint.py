@@ -2,11 +2,13 @@
 
 The reference has no differentiation (no ForwardDiff / ChainRulesCore in its manifests, and its
 SRT hard-types τ as Float64).  This module exposes the discrete adjoint of the device kernels for
-D2Q9 / D2Q13 lattices with SRT or TRT, a uniform force and bounce-back / moving-wall boundaries:
+D2Q9 / D2Q13 lattices with SRT, TRT or regularised MRT, a uniform force and bounce-back /
+moving-wall boundaries:
 
     L(u0, τ, F) = Σ_x |u(f_T) - u*|²,   f_0 = f_eq(1, u0),   f_{t+1} = apply!(stream(collide(f_t; τ, F))),
 
-`AdjointProblem.run(u0, u_target)` returns L, ∂L/∂τ_s, ∂L/∂τ_a, ∂L/∂F and ∂L/∂u0 (binomial
+`AdjointProblem.run(u0, u_target)` returns L, ∂L/∂τ_s, ∂L/∂τ_a, ∂L/∂F and ∂L/∂u0 (MRT: "dtau_s" is
+∂L/∂τ_2, the second-order relaxation time, which also scales the force shift; "dtau_a" is 0) (binomial
 checkpointing with a given number of state slots, one CUDA graph).  `LBMLoss` wraps it as a torch.autograd.Function, the Python
 counterpart of a ChainRulesCore.rrule for `simulate`.
 """

@@ -1,5 +1,5 @@
 // lbm_adjoint.cu -- instantiations and launcher of the adjoint kernels (lbm_adjoint.cuh) for
-// D2Q9 and D2Q13 (second-order equilibria), SRT and TRT, FP64 and FP32-deviation storage.
+// D2Q9 and D2Q13 (second-order equilibria), SRT, TRT and MRT, FP64 and FP32-deviation storage.
 #include "lbm_adjoint.cuh"
 
 namespace lbm {
@@ -22,6 +22,10 @@ cudaError_t adj_run(int op, int coll, const StepParams<typename S::C>& p, AdjArg
     case ADJ_STEP:
       if (coll == LBM_TRT)
         launch_after_prior(adj_step_kernel<L, S, LBM_TRT>, dim3(nblocks), dim3(kAdjThreads), s, p, a,
+                           static_cast<const T*>(src), pull, static_cast<const T*>(lam_next),
+                           static_cast<T*>(lam_out), slots);
+      else if (coll == LBM_MRT)
+        launch_after_prior(adj_step_kernel<L, S, LBM_MRT>, dim3(nblocks), dim3(kAdjThreads), s, p, a,
                            static_cast<const T*>(src), pull, static_cast<const T*>(lam_next),
                            static_cast<T*>(lam_out), slots);
       else

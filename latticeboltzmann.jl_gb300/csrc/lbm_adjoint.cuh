@@ -1,8 +1,8 @@
 // lbm_adjoint.cuh -- reverse-mode (adjoint) kernels of the fused collide-stream step.
 //
 // The reference has no differentiation; this is the discrete adjoint of the forward map the
-// kernels implement, for lattices with SRT or TRT collision, a uniform force and the boundary
-// conditions (bounce-back, moving wall):
+// kernels implement, for lattices with SRT, TRT or (second-order sets) regularised MRT collision, a
+// uniform force and the boundary conditions (bounce-back, moving wall):
 //
 //   A_{t+1} = S C(A_t; τ_s, τ_a, F),  A_0 = f_eq(ρ = 1, u0),  L = Σ_x |u(A_T) - u*|²,
 //
@@ -20,6 +20,7 @@
 // where P_s / P_a are the symmetric / antisymmetric parts over opposite pairs (trt.jl:71-94).
 // Parameter sensitivities accumulate μ^T ∂C/∂θ per node: -Σ μ^s (f - f_eq) for ω_s,
 // -Σ μ^a (f - f_eq) for ω_a, Σ_a G_a F_a for τ_a through the force shift, τ_a G_a for F_a.
+// The MRT collision's transpose is formed through its moments instead (adj_mrt_node).
 // Sums are FP64, one slot per block, blocks always own the same nodes (deterministic).
 #pragma once
 
@@ -156,6 +157,69 @@ __device__ __forceinline__ bool bc_replaces(const StepParams<CT>& p, int x, int 
   return false;
 }
 
+// J_C^T μ of the regularised MRT collision of a second-order set (mrt.jl:56-118 with N = 2), in
+// the form the forward kernel evaluates it (mrt_coeffs):
+//   M_ab = Σ_i f_i c_x^a c_y^b,  ρ = M_00 (+1 in deviation form),  u' = M_1/ρ + τ_2 F,
+//   X = M_2 - M_00 I / κ (the Hermite coefficient a_f),  E = ρ u'u' (a_eq),  A = (1-ω) X + ω E,
+//   f_out,i = w_i (M_00 - κ tr A / 2 + κ²/2 (A_xx c_x² + 2 A_xy c_x c_y + A_yy c_y²))
+//             + W1_i (c_x ρu'_x + c_y ρu'_y),
+// with ω = 1/τ_2, κ = 1/c_s² (the reference's speed_of_sound_squared), W1_i = κ w_i (FP64) or the
+// momentum-exact w1_i (deviation form).  Reverse:
+// Λ = Σ_i μ_i w_i (1, c_x², c_x c_y, c_y²) and Σ_i μ_i W1_i c_i give ∂L/∂A, ∂L/∂(ρu'), then
+// ∂L/∂M_ab through ρ, u' and X, and λ_i = Σ_ab ∂L/∂M_ab c_x^a c_y^b.  Parameters: ∂A/∂ω = E - X
+// (slot 0), ∂u'/∂τ_2 = F through the force shift (slot 2), ∂u'/∂F = τ_2 (slots 3, 4).
+template <class L, class S>
+__device__ __forceinline__ void adj_mrt_node(const StepParams<typename S::C>& p, const typename S::C* f,
+                                             const typename S::C* mu, typename S::C Fx, typename S::C Fy,
+                                             typename S::C shift, typename S::C sFx, typename S::C sFy,
+                                             typename S::C* tacc, typename S::T* __restrict__ lam_out, long long node) {
+  static_assert(L::HN == 2, "the MRT adjoint covers second-order velocity sets");
+  using CT = typename S::C;
+  CT M0 = 0, M1 = 0, M2 = 0, M3 = 0, M4 = 0, M5 = 0;
+  CT L0 = 0, L3 = 0, L4 = 0, L5 = 0, Lx = 0, Ly = 0;
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr CT cx = (CT)L::cx(i), cy = (CT)L::cy(i);
+    M0 += f[i];
+    M1 += cx * f[i];
+    M2 += cy * f[i];
+    M3 += (cx * cx) * f[i];
+    M4 += (cx * cy) * f[i];
+    M5 += (cy * cy) * f[i];
+    const CT wm = p.w[i] * mu[i];
+    const CT w1m = (S::DEV ? p.w1[i] : p.w[i] * p.cs) * mu[i];
+    L0 += wm;
+    L3 += (cx * cx) * wm;
+    L4 += (cx * cy) * wm;
+    L5 += (cy * cy) * wm;
+    Lx += cx * w1m;
+    Ly += cy * w1m;
+  });
+  const CT rho = S::DEV ? (CT)1 + M0 : M0;
+  const CT inv_rho = (CT)1 / rho;
+  const CT vx = M1 * inv_rho, vy = M2 * inv_rho;
+  const CT ux = vx + sFx, uy = vy + sFy;
+  const CT om = p.mrt_b[1], am = p.mrt_a[1];
+  const CT ics = (CT)1 / p.cs, c2 = p.cs * p.cs * (CT)0.5;
+  const CT gxx = c2 * (L3 - ics * L0), gyy = c2 * (L5 - ics * L0), gxy = (CT)2 * c2 * L4;
+  tacc[0] += gxx * (rho * ux * ux - (M3 - ics * M0)) + gxy * (rho * ux * uy - M4) + gyy * (rho * uy * uy - (M5 - ics * M0));
+  const CT gux = om * rho * ((CT)2 * ux * gxx + uy * gxy) + rho * Lx;
+  const CT guy = om * rho * (ux * gxy + (CT)2 * uy * gyy) + rho * Ly;
+  const CT grho = om * (ux * ux * gxx + ux * uy * gxy + uy * uy * gyy) + ux * Lx + uy * Ly -
+                  (gux * vx + guy * vy) * inv_rho;
+  const CT gM0 = L0 - am * ics * (gxx + gyy) + grho;
+  const CT gM1 = gux * inv_rho, gM2 = guy * inv_rho, gM3 = am * gxx, gM4 = am * gxy, gM5 = am * gyy;
+  tacc[2] += gux * Fx + guy * Fy;
+  tacc[3] += shift * gux;
+  tacc[4] += shift * guy;
+  static_for<0, L::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr CT cx = (CT)L::cx(i), cy = (CT)L::cy(i);
+    const CT l = gM0 + gM1 * cx + gM2 * cy + gM3 * (cx * cx) + gM4 * (cx * cy) + gM5 * (cy * cy);
+    lam_out[(size_t)i * p.n + node] = (typename S::T)l;
+  });
+}
+
 // One reverse step: λ_t = J_C(A_t)^T S^T λ_{t+1}.  A_t is pulled from B_{t-1} (pull = true) or
 // read locally (A_0).  Parameter sensitivities are added to this block's slots.
 template <class L, class S, int COLL>
@@ -206,6 +270,10 @@ __global__ void __launch_bounds__(kAdjThreads, (S::DEV && L::Q <= 9) ? 4 : 1) ad
           mu[i] = m;
         }
       });
+    }
+    if constexpr (COLL == LBM_MRT) {
+      adj_mrt_node<L, S>(p, f, mu, Fx, Fy, shift, sFx, sFy, tacc, lam_out, node);
+      continue;
     }
     // moments, equilibrium and its velocity derivatives (as the forward collision forms them)
     CT s = 0, jx = 0, jy = 0;

@@ -1891,7 +1891,8 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
   if (!out || !c || nsteps < 1 || slots < 0) return LBM_ERR_INVALID;
   *out = nullptr;
   if (c->qid != LBM_D2Q9 && c->qid != LBM_D2Q13) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: D2Q9 / D2Q13 only");
-  if (c->coll != LBM_SRT && c->coll != LBM_TRT) return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: SRT / TRT only");
+  if (c->coll != LBM_SRT && c->coll != LBM_TRT && c->coll != LBM_MRT)
+    return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: SRT / TRT / MRT only");
   if (c->storage != LBM_STORE_F64 && c->storage != LBM_STORE_F32_DEV)
     return fail(c, LBM_ERR_UNSUPPORTED, "adjoint: FP64 or FP32-deviation storage only");
   if (c->force_kind != LBM_FORCE_NONE && c->force_kind != LBM_FORCE_CONSTANT)
@@ -1997,9 +1998,11 @@ int32_t lbm_adjoint_run(lbm_adjoint* a, const double* u0, const double* u_target
   if (grad_u0 && cudaMemcpyAsync(grad_u0, a->d_grad, vb, cudaMemcpyDefault, s) != cudaSuccess)
     return afail(a, LBM_ERR_CUDA, "adjoint: gradient copy");
   if (cudaStreamSynchronize(s) != cudaSuccess) return afail(a, LBM_ERR_CUDA, "adjoint: synchronize");
-  // result: loss, dL/dτ_s, dL/dτ_a, dL/dF_x, dL/dF_y (partial derivatives; SRT: dL/dτ in [1] and [2] summed)
+  // result: loss, dL/dτ_s, dL/dτ_a, dL/dF_x, dL/dF_y (partial derivatives; SRT: dL/dτ in [1] and [2] summed;
+  // MRT: dL/dτ_2 in [1], the second-order relaxation time, which also scales the force shift)
   const double* h = a->h_out;
-  const double ts = c->coll == LBM_TRT ? 1.0 / c->pd.inv_ts : 1.0 / c->pd.om_b;
+  const double ts = c->coll == LBM_TRT ? 1.0 / c->pd.inv_ts
+                  : c->coll == LBM_MRT ? 1.0 / c->pd.mrt_b[1] : 1.0 / c->pd.om_b;
   const double ta = c->coll == LBM_TRT ? 1.0 / c->pd.inv_ta : ts;
   result[0] = h[0];
   if (c->coll == LBM_TRT) {

@@ -753,6 +753,46 @@ static void collide_srt_trt_node(const Quad& q, int kind, R tau0, R tau1, bool f
   }
 }
 
+// One node of the MRT collide! of a second-order set (mrt.jl:56-118 with N = div(order, 2) = 2:
+// D2Q9, D2Q13) for any number type R, operation for operation the double path of collide()
+// below: tau1, tau2 are τs[1], τs[2]; the force shift uses τs[2] (mrt.jl:91-95); the first-order
+// coefficient a_coll[1] is formed there but never used, so it is skipped.  Hs: the Hermite tables
+// of collide() (mrt.jl:29-34).
+template <class R>
+static void collide_mrt2_node(const Quad& q, const double (*Hs)[37][16], R tau1, R tau2, bool force, R Fx, R Fy,
+                              const R* f, R* out) {
+  (void)tau1;
+  const int Q = q.Q;
+  const double cs = q.cs;
+  const R rho = density(q, f);
+  R u[2];
+  velocity(q, f, rho, u);
+  if (force) {
+    u[0] = u[0] + tau2 * Fx;
+    u[1] = u[1] + tau2 * Fy;
+  }
+  R aeq[4], af[4], acoll[4];
+  for (int b = 0; b < 2; ++b)  // equilibrium_coefficient(Val{2}, q, ρ, u, T = 1): hermite.jl:37-77
+    for (int a = 0; a < 2; ++a) {
+      R m = u[a] * u[b];
+      if (a == b) m = m + 0.0;
+      aeq[a + 2 * b] = rho * m;
+    }
+  for (int k = 0; k < 4; ++k) {
+    R sm = f[0] * Hs[2][0][k];
+    for (int i = 1; i < Q; ++i) sm = sm + f[i] * Hs[2][i][k];
+    af[k] = sm;
+  }
+  for (int k = 0; k < 4; ++k) acoll[k] = (1 - 1 / tau2) * af[k] + (1 / tau2) * aeq[k];
+  for (int i = 0; i < Q; ++i) {
+    const R first = cs * rho * (u[0] * Hs[1][i][0] + u[1] * Hs[1][i][1]);
+    R dot = 0.0;
+    for (int k = 0; k < 4; ++k) dot += acoll[k] * Hs[2][i][k];
+    const R hi = std::pow(cs, 2) * dot / factorial(2);
+    out[i] = q.w[i] * ((rho + first) + hi);
+  }
+}
+
 // collide! for SRT (srt.jl:18-62), TRT (trt.jl:42-97), MRT (mrt.jl:49-118), and the
 // iterative-initialisation model (iterative_initialization.jl:41-60).  Loop order x outer,
 // y inner, as in the reference.
@@ -1463,8 +1503,9 @@ int orc_run(int qid, const orc_problem* p, const orc_collision* cm, int nbc, con
 
 // Forward-mode derivative of a field loss through the time loop, for the gradient checks of
 // the adjoint: f_0 = equilibrium(1, u0) per node (maxwell_boltzmann_equilibrium.jl:12-66),
-// then `nsteps` times collide! (SRT kind 0 / TRT kind 1 with the uniform lattice force F, as
-// srt.jl:18-62 / trt.jl:42-97) and the periodic stream! (stream.jl:18-30), and
+// then `nsteps` times collide! (SRT kind 0 / TRT kind 1 / MRT kind 2 of a second-order set, with
+// the uniform lattice force F, as srt.jl:18-62 / trt.jl:42-97 / mrt.jl:56-118; MRT: tau = (τs[1],
+// τs[2])) and the periodic stream! (stream.jl:18-30), and
 //     L = Σ_nodes (u_x - ut_x)² + (u_y - ut_y)²,   u = velocity!(f_T) (moments.jl:1-19).
 // Every value is a Dual whose derivative part is seeded with the direction
 // (dτ_0, dτ_1, dF_x, dF_y) = seed and du0 for u0 (null: zero), so out = (L, dL/dε along it).
@@ -1472,9 +1513,17 @@ int orc_run(int qid, const orc_problem* p, const orc_collision* cm, int nbc, con
 int orc_tangent_loss(int qid, int kind, const double* tau, const double* F, int nx, int ny, const double* u0,
                      const double* ut, const double* seed, const double* du0, long nsteps, int nthreads,
                      const orc_bc* bcs, int nbc, double* out) {
-  if ((kind != 0 && kind != 1) || nx <= 0 || ny <= 0 || nsteps < 0 || nbc < 0 || (nbc > 0 && !bcs)) return -1;
+  if (kind < 0 || kind > 2 || nx <= 0 || ny <= 0 || nsteps < 0 || nbc < 0 || (nbc > 0 && !bcs)) return -1;
   const std::vector<orc_bc> bclist(bcs, bcs + nbc);
   const Quad q = make_quad(qid);
+  if (kind == 2 && q.order / 2 != 2) return -1;
+  double Hs[5][37][16];
+  if (kind == 2)
+    for (int nh = 1; nh <= 2; ++nh)
+      for (int i = 0; i < q.Q; ++i) {
+        const int xi[2] = {q.cx[i], q.cy[i]};
+        hermite_q(nh, xi, 1.0 / q.cs, Hs[nh][i]);
+      }
   const int Q = q.Q;
   const size_t nn = (size_t)nx * ny, n = nn * Q;
   auto idx = [&](int x, int y, int i) { return (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * i); };
@@ -1495,7 +1544,8 @@ int orc_tangent_loss(int qid, int kind, const double* tau, const double* F, int 
       Dual f[37], o[37];
       for (int y = 0; y < ny; ++y) {
         for (int i = 0; i < Q; ++i) f[i] = a[idx(x, y, i)];
-        collide_srt_trt_node<Dual>(q, kind, t0, t1, force, Fx, Fy, f, o);
+        if (kind == 2) collide_mrt2_node<Dual>(q, Hs, t0, t1, force, Fx, Fy, f, o);
+        else collide_srt_trt_node<Dual>(q, kind, t0, t1, force, Fx, Fy, f, o);
         for (int i = 0; i < Q; ++i) b[idx(x, y, i)] = o[i];
       }
     }

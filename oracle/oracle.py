@@ -383,7 +383,8 @@ def run(q, p, cm, bcs, f0, t_first, t_last, dt=0.0, nthreads=1):
 
 def tangent_loss(q, kind, taus, F, u0, ut, nsteps, seed=(0.0, 0.0, 0.0, 0.0), du0=None, nthreads=1, bcs=()):
     """L = Σ |u(f_T) - ut|² after `nsteps` collide → periodic stream → apply!(bcs) steps from
-    f_0 = equilibrium(1, u0) (SRT `kind` "SRT" with τ = taus[0], TRT with τ_s, τ_a = taus, uniform
+    f_0 = equilibrium(1, u0) (SRT `kind` "SRT" with τ = taus[0], TRT with τ_s, τ_a = taus, MRT of a
+    second-order set with τs[1], τs[2] = taus (the outputs depend on τs[2] only), uniform
     lattice force F, the boundary conditions `bcs` built by bc()), and its forward-mode derivative
     along seed = (dτ_0, dτ_1, dF_x, dF_y) and the u0 direction du0, propagated with dual numbers.
     u0, ut, du0: shape (2, ny, nx).  Returns (L, dL)."""
@@ -398,7 +399,7 @@ def tangent_loss(q, kind, taus, F, u0, ut, nsteps, seed=(0.0, 0.0, 0.0, 0.0), du
     t = np.array([float(taus[0]), float(taus[1] if len(taus) > 1 else taus[0])])
     out = np.zeros(2)
     arr = (OrcBC * max(1, len(bcs)))(*bcs)
-    rc = lib().orc_tangent_loss(qid(q), {"SRT": 0, "TRT": 1}[kind], t, np.array(F, dtype=np.float64), nx, ny,
+    rc = lib().orc_tangent_loss(qid(q), {"SRT": 0, "TRT": 1, "MRT": 2}[kind], t, np.array(F, dtype=np.float64), nx, ny,
                                 u0, ut, np.array(seed, dtype=np.float64),
                                 d.ctypes.data if d is not None else None, int(nsteps), int(nthreads),
                                 C.cast(arr, C.c_void_p) if len(bcs) else None, len(bcs), out)

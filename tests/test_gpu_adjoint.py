@@ -296,3 +296,81 @@ def test_walled_adjoint_matches_oracle_forward_mode(lbm_gpu, O, lid):
                    (res["dF"][0], tangent((0, 0, 1, 0))[1]),
                    (float(np.sum(res["grad_u0"] * v)), tangent((0, 0, 0, 0), v)[1])]:
         assert ad == pytest.approx(fm, rel=1e-8), (ad, fm)
+
+
+@pytest.mark.parametrize("qname,bc", [("D2Q9", "none"), ("D2Q9", "walls"), ("D2Q9", "lid"), ("D2Q13", "none")])
+def test_mrt_adjoint_matches_oracle_forward_mode(lbm_gpu, O, qname, bc):
+    """Regularised MRT (mrt.jl:56-118; a second-order set relaxes its second-order Hermite
+    coefficient with τ_2, which also scales the force shift): the adjoint's ∂L/∂τ_2, ∂L/∂F and a
+    directional ∂L/∂u0 against the forward-mode derivatives of the oracle's loop, periodic, with
+    channel walls and as a lid-driven cavity (≤ 1e-8)."""
+    lbm = lbm_gpu
+    q = lbm.Quadratures[qname]
+    u0, ut = _fields(lbm)
+    tau, F = 0.8, (2e-6, -1e-6) if bc == "none" else (2e-6, 0.0)
+    bcs = () if bc == "none" else _walls(lbm, lid=(bc == "lid"))
+    obcs = () if bc == "none" else _owalls(O, lid=(bc == "lid"))
+    prob = lbm.AdjointProblem(q, NX, NY, lbm.MRT(q, tau), force=F, nsteps=STEPS, slots=5,
+                              boundary_conditions=bcs)
+    res = prob.run(u0, ut)
+    prob.close()
+    v = np.random.default_rng(23).normal(size=u0.shape)
+
+    def tangent(seed, du0=None):
+        return O.tangent_loss(qname, "MRT", (tau, tau), F, u0, ut, STEPS, seed=seed, du0=du0, bcs=obcs,
+                              nthreads=O.max_threads())
+
+    L, d_tau = tangent((0, 1, 0, 0))
+    assert res["loss"] == pytest.approx(L, rel=1e-10)
+    assert tangent((1, 0, 0, 0))[1] == 0.0  # the first-order relaxation time never reaches the outputs
+    pairs = [(res["dtau_s"], d_tau), (res["dF"][0], tangent((0, 0, 1, 0))[1]),
+             (float(np.sum(res["grad_u0"] * v)), tangent((0, 0, 0, 0), v)[1])]
+    if bc == "none":
+        pairs.append((res["dF"][1], tangent((0, 0, 0, 1))[1]))
+    assert res["dtau_a"] == 0.0
+    for ad, fm in pairs:
+        assert ad == pytest.approx(fm, rel=1e-8), (ad, fm)
+
+
+def test_mrt_adjoint_matches_finite_differences(lbm_gpu):
+    """∂L/∂τ, ∂L/∂F_x and a directional ∂L/∂u0 of the MRT channel with walls against fourth-order
+    central differences of the device forward model (FP64)."""
+    lbm = lbm_gpu
+    q = lbm.D2Q9()
+    u0, ut = _fields(lbm)
+    tau, Fx = 0.8, 2e-6
+
+    def loss(t, fx, u):
+        p = lbm.AdjointProblem(q, NX, NY, lbm.MRT(q, t), force=(fx, 0.0), nsteps=STEPS,
+                               boundary_conditions=_walls(lbm))
+        L = p.loss(u, ut)
+        p.close()
+        return L
+
+    def fd(fun, h):
+        return (fun(-2 * h) - 8 * fun(-h) + 8 * fun(h) - fun(2 * h)) / (12 * h)
+
+    prob = lbm.AdjointProblem(q, NX, NY, lbm.MRT(q, tau), force=(Fx, 0.0), nsteps=STEPS,
+                              boundary_conditions=_walls(lbm))
+    res = prob.run(u0, ut)
+    prob.close()
+    v = np.random.default_rng(29).normal(size=u0.shape)
+    for ad, ref in [(res["dtau_s"], fd(lambda e: loss(tau + e, Fx, u0), 1e-4)),
+                    (res["dF"][0], fd(lambda e: loss(tau, Fx + e, u0), 1e-7)),
+                    (float(np.sum(res["grad_u0"] * v)), fd(lambda e: loss(tau, Fx, u0 + e * v), 1e-5))]:
+        assert abs(ad - ref) <= 1e-6 * max(abs(ref), 1e-12), (ad, ref)
+
+
+def test_mrt_fp32_adjoint_close_to_fp64(lbm_gpu):
+    lbm = lbm_gpu
+    q = lbm.D2Q9()
+    u0, ut = _fields(lbm)
+    r = {}
+    for st in ("f64", "f32dev"):
+        prob = lbm.AdjointProblem(q, NX, NY, lbm.MRT(q, 0.8), force=(2e-6, -1e-6), nsteps=STEPS, storage=st)
+        r[st] = prob.run(u0, ut)
+        prob.close()
+    assert r["f32dev"]["loss"] == pytest.approx(r["f64"]["loss"], rel=1e-4)
+    assert r["f32dev"]["dtau_s"] == pytest.approx(r["f64"]["dtau_s"], rel=1e-3)
+    g64, g32 = r["f64"]["grad_u0"], r["f32dev"]["grad_u0"]
+    assert np.max(np.abs(g32 - g64)) <= 1e-3 * np.max(np.abs(g64))

@@ -31,7 +31,8 @@ def _double_loop_loss(O, q, kind, taus, u0, ut, steps):
     return float(np.sum((ux - ut[0]) ** 2 + (uy - ut[1]) ** 2))
 
 
-@pytest.mark.parametrize("q,kind", [("D2Q9", "TRT"), ("D2Q9", "SRT"), ("D2Q13", "TRT")])
+@pytest.mark.parametrize("q,kind", [("D2Q9", "TRT"), ("D2Q9", "SRT"), ("D2Q13", "TRT"), ("D2Q9", "MRT"),
+                                    ("D2Q13", "MRT")])
 def test_value_part_is_the_double_loop(lbm, O, q, kind):
     u0, ut = _fields(lbm)
     taus = (0.8, 1.1)
@@ -39,7 +40,8 @@ def test_value_part_is_the_double_loop(lbm, O, q, kind):
     assert L == pytest.approx(_double_loop_loss(O, q, kind, taus, u0, ut, STEPS), rel=1e-13)
 
 
-@pytest.mark.parametrize("q,kind", [("D2Q9", "TRT"), ("D2Q9", "SRT"), ("D2Q13", "TRT")])
+@pytest.mark.parametrize("q,kind", [("D2Q9", "TRT"), ("D2Q9", "SRT"), ("D2Q13", "TRT"), ("D2Q9", "MRT"),
+                                    ("D2Q13", "MRT")])
 def test_tangents_match_central_differences(lbm, O, q, kind):
     u0, ut = _fields(lbm)
     taus, F = [0.8, 1.1], [2e-6, -1e-6]
@@ -56,7 +58,7 @@ def test_tangents_match_central_differences(lbm, O, q, kind):
               ((0, 0, 1, 0), None, fd(lambda e: value(dfx=e), 1e-7)),
               ((0, 0, 0, 1), None, fd(lambda e: value(dfy=e), 1e-7)),
               ((0, 0, 0, 0), v, fd(lambda e: value(du=e), 1e-5))]
-    if kind == "TRT":
+    if kind in ("TRT", "MRT"):  # MRT of a second-order set: the outputs depend on τs[2] only
         checks.append(((0, 1, 0, 0), None, fd(lambda e: value(dt1=e), 1e-4)))
     for seed, du0, ref in checks:
         _, d = O.tangent_loss(q, kind, taus, F, u0, ut, STEPS, seed=seed, du0=du0)
@@ -93,14 +95,15 @@ def test_walled_value_part_is_the_double_loop(lbm, O, lid):
     assert L == pytest.approx(ref, rel=1e-13)
 
 
-def test_walled_tangents_match_central_differences(lbm, O):
+@pytest.mark.parametrize("kind", ["TRT", "MRT"])
+def test_walled_tangents_match_central_differences(lbm, O, kind):
     u0, ut = _fields(lbm)
     q, taus, F = "D2Q9", [0.8, 1.1], [2e-6, 0.0]
     bcs = _walls(O)
     v = np.random.default_rng(6).normal(size=u0.shape)
 
     def value(dt0=0.0, dt1=0.0, dfx=0.0, du=0.0):
-        return O.tangent_loss(q, "TRT", (taus[0] + dt0, taus[1] + dt1), (F[0] + dfx, F[1]), u0 + du * v, ut, STEPS,
+        return O.tangent_loss(q, kind, (taus[0] + dt0, taus[1] + dt1), (F[0] + dfx, F[1]), u0 + du * v, ut, STEPS,
                               bcs=bcs)[0]
 
     def fd(fun, h):
@@ -110,5 +113,5 @@ def test_walled_tangents_match_central_differences(lbm, O):
                            ((0, 1, 0, 0), None, fd(lambda e: value(dt1=e), 1e-4)),
                            ((0, 0, 1, 0), None, fd(lambda e: value(dfx=e), 1e-7)),
                            ((0, 0, 0, 0), v, fd(lambda e: value(du=e), 1e-5))]:
-        _, d = O.tangent_loss(q, "TRT", taus, F, u0, ut, STEPS, seed=seed, du0=du0, bcs=bcs)
+        _, d = O.tangent_loss(q, kind, taus, F, u0, ut, STEPS, seed=seed, du0=du0, bcs=bcs)
         assert d == pytest.approx(ref, rel=1e-6, abs=1e-13), (seed, d, ref)
