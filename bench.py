@@ -568,15 +568,19 @@ def main():
 
     e2e = None
     if not args.profile:
-        e2e_s, h2d, d2h = time_e2e(torch, lbm, problem, model, f0, args.steps, dt)
-        e2e_s = max_over_ranks(e2e_s, world, "cuda")
+        # three complete end-to-end sequences, the median reported: the host link is shared with
+        # the machine's other GPUs, so a single sequence can catch a neighbour's transfers
+        runs = [time_e2e(torch, lbm, problem, model, f0, args.steps, dt) for _ in range(3)]
+        e2e_runs = [max_over_ranks(r[0], world, "cuda") for r in runs]
+        e2e_s, h2d, d2h = sorted(e2e_runs)[1], runs[0][1], runs[0][2]
         # the drop-in call sequence of simulate(model, 0:K): the populations uploaded from pinned host
         # memory once before the K steps and downloaded once after them (the state stays resident
         # in between, as the reference keeps it in f_stream); bytes per step are those totals / K
         e2e = {"value": job_mlups(NX * NY * args.steps, e2e_s, world), "unit": "MLUPS",
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                "h2d_bytes_per_call": h2d, "d2h_bytes_per_call": d2h,
-               "copies": "one upload before and one download after the K-step lbm_step call"}
+               "copies": "one upload before and one download after the K-step lbm_step call",
+               "runs_s": e2e_runs, "reported": "median of three complete sequences"}
     model.close()
 
     extra = {}
