@@ -89,3 +89,25 @@ def test_unsupported_combinations(lbm_gpu):
     assert L.lbm_collide_device(f16.h, None, None, 0.0) in (N.LBM_ERR_INVALID, N.LBM_ERR_UNSUPPORTED)
     for lat in (a, b, c, d17, f16):
         lat.close()
+
+
+@pytest.mark.parametrize("storage", ["f32sr", "f64dd", "f16dev"])
+def test_single_lattice_storages_refuse_batches_and_the_adjoint(lbm_gpu, storage):
+    """The stochastically rounded FP32, the FP64-storage float-float and the FP16 storages step
+    single lattices only: a batch of them and an adjoint on them are refused with
+    LBM_ERR_UNSUPPORTED, and the lattices stay usable."""
+    lbm = lbm_gpu
+    N = lbm._native
+    L = N.lib()
+    a, b = _lattice(lbm, storage=storage), _lattice(lbm, storage=storage)
+    with pytest.raises(N.LbmError) as err:
+        lbm.DeviceBatch([a, b])
+    assert err.value.status == N.LBM_ERR_UNSUPPORTED
+    h = C.c_void_p()
+    assert L.lbm_adjoint_create(C.byref(h), a.h, 10, 0) == N.LBM_ERR_UNSUPPORTED
+    assert b"adjoint" in L.lbm_last_error(a.h)
+    a.initialize_fields()
+    a.step(3)
+    assert np.all(np.isfinite(a.download()))
+    a.close()
+    b.close()
