@@ -49,10 +49,11 @@ inline void launch_step(const OpArgs& a, const StepParams<typename S::C>& p) {
   auto* dst = static_cast<typename S::T*>(a.dst);
   // SRT / TRT of the deviation storages: two nodes per thread on packed FP32 pairs (even nx).
   // Where the pair kernel's registers would cut the occupancy too far, the one-node kernel stays:
-  // D2Q37 in FP32 / FP16 (154 registers against 72, measured 8 % slower), and float-float
-  // arithmetic (DF64 and FP32-SR storage) above D2Q9 (D2Q13: 126 against 56).
-  constexpr bool kPairs =
-      MODE == 1 && S::DEV && (std::is_same<typename S::C, dd>::value ? L::Q <= 9 : L::Q <= 25);
+  // D2Q37 in FP32 / FP16 (154 registers against 72, measured 8 % slower), float-float DF64
+  // above D2Q17 (D2Q13 and D2Q17 measured 4 % faster as pairs, D2Q21 and D2Q37 no faster), and
+  // the other float-float storages (FP32-SR, FP64-DD) above D2Q9.
+  constexpr int kPairMaxQ = std::is_same<typename S::C, dd>::value ? (S::id == LBM_STORE_DF64_DEV ? 17 : 9) : 25;
+  constexpr bool kPairs = MODE == 1 && S::DEV && L::Q <= kPairMaxQ;
   if constexpr (kPairs) {
     if ((a.coll == LBM_SRT || a.coll == LBM_TRT) && p.nx % 2 == 0) {
       const dim3 g2((unsigned)((p.nx / 2 + kBlockX - 1) / kBlockX), g.y);
