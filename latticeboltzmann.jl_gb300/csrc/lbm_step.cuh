@@ -747,15 +747,18 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
 // loaded, and all outputs stored, as one aligned two-node access; away from the x edges the
 // second node's addresses are the first's plus one element.  Nodes within R of an x edge, or of
 // a y edge when boundary conditions are set, are pulled by load_streamed.  Needs nx even.
-// Residency: FP16 D2Q4-D2Q9 ten blocks per SM (48 registers), F64DD six (80 registers, a few
-// spilled words: 16.4 against 15.3 GLUPS at 103 registers and four blocks, D2Q9 4096^2).
+// Residency: FP16 D2Q4-D2Q9 ten blocks per SM (48 registers), F64DD seven (72 registers, a few
+// spilled words: 20.9 against 20.5 GLUPS at six blocks, D2Q9 4096^2).
 template <class L, class S>
-__global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <= 9) ? 10 : (S::id == LBM_STORE_F64_DD ? 6 : 0)) step_pair_kernel(StepParams<typename S::C> p,
+__global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <= 9) ? 10 : (S::id == LBM_STORE_F64_DD ? 7 : 0)) step_pair_kernel(StepParams<typename S::C> p,
                                                             const typename S::T* __restrict__ src,
                                                             typename S::T* __restrict__ dst) {
   using T = typename S::T;
   using C = typename S::C;
   using P = typename Packed<C>::type;
+  // FP64-DD: per-thread staging slots of the Q population pairs (16 B each; no thread reads
+  // another's, so no barrier), which let the double <-> float-float conversions run in loops
+  __shared__ double2 wide_stage[S::WIDE ? L::Q : 1][S::WIDE ? kBlockX : 1];
   wait_prior_grid();
   const int x0 = 2 * (int)(blockIdx.x * kBlockX + threadIdx.x);
   if (x0 >= p.nx) return;
@@ -772,13 +775,35 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
         ys += (ys < 0) ? p.ny : 0;
         yo[k] = ys * p.nx;
       }
-      static_for<0, L::Q>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        const T* a = src + plane_off(p, i) + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
-        if constexpr (S::WIDE) v[i] = pack2(load_pop<S>(p, a, i), load_pop<S>(p, a + 1, i));
-        else if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
-        else v[i] = pack2(S::ld(a), S::ld(a + 1));
-      });
+      if constexpr (S::WIDE) {
+        // the raw doubles of both nodes go to this thread's staging slots (all loads in flight at
+        // once), one loop converts them in place: one copy of the split code instead of 2 Q
+        static_for<0, L::Q>([&](auto I) {
+          constexpr int i = decltype(I)::value;
+          const T* a = src + plane_off(p, i) + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
+          wide_stage[i][threadIdx.x] = make_double2(a[0], a[1]);
+        });
+#pragma unroll 1
+        for (int i = 0; i < L::Q; ++i) {
+          const double2 f = wide_stage[i][threadIdx.x];
+          const pdd g = pack2(S::from_f(f.x, p.wf[i]), S::from_f(f.y, p.wf[i]));
+          wide_stage[i][threadIdx.x] = make_double2(__longlong_as_double((long long)g.hi.r),
+                                                    __longlong_as_double((long long)g.lo.r));
+        }
+        static_for<0, L::Q>([&](auto I) {
+          constexpr int i = decltype(I)::value;
+          const double2 g = wide_stage[i][threadIdx.x];
+          v[i].hi.r = (unsigned long long)__double_as_longlong(g.x);
+          v[i].lo.r = (unsigned long long)__double_as_longlong(g.y);
+        });
+      } else {
+        static_for<0, L::Q>([&](auto I) {
+          constexpr int i = decltype(I)::value;
+          const T* a = src + plane_off(p, i) + (yo[L::R + L::cy(i)] + x0 - L::cx(i));
+          if constexpr (L::cx(i) == 0) v[i] = S::ld2(a);
+          else v[i] = pack2(S::ld(a), S::ld(a + 1));
+        });
+      }
     } else {
       C a[L::Q], b[L::Q];
       load_streamed<L, S>(p, src, x0, y, a);
@@ -803,11 +828,22 @@ __global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <
         const float a = round_stochastic(v[i].hi.lo(), v[i].lo.lo(), sr_bits(node, i, step));
         const float b = round_stochastic(v[i].hi.hi(), v[i].lo.hi(), sr_bits(node + 1, i, step));
         *reinterpret_cast<unsigned long long*>(dst + plane_off(p, i) + node) = pf2(a, b).r;
-      } else if constexpr (S::WIDE) {  // both lanes as one aligned 16-byte store
-        *reinterpret_cast<double2*>(dst + plane_off(p, i) + node) =
-            make_double2(S::to_f(dd(v[i].hi.lo(), v[i].lo.lo()), p.wf[i]), S::to_f(dd(v[i].hi.hi(), v[i].lo.hi()), p.wf[i]));
+      } else if constexpr (S::WIDE) {  // staged: one loop below forms and stores the doubles
+        wide_stage[i][threadIdx.x] = make_double2(__longlong_as_double((long long)v[i].hi.r),
+                                                  __longlong_as_double((long long)v[i].lo.r));
       } else {
         S::st2(dst + plane_off(p, i) + node, v[i]);
+      }
+    }
+    if constexpr (S::WIDE) {  // both lanes as one aligned 16-byte store per population
+#pragma unroll 1
+      for (int i = 0; i < L::Q; ++i) {
+        const double2 g = wide_stage[i][threadIdx.x];
+        pdd vi;
+        vi.hi.r = (unsigned long long)__double_as_longlong(g.x);
+        vi.lo.r = (unsigned long long)__double_as_longlong(g.y);
+        *reinterpret_cast<double2*>(dst + plane_off(p, i) + node) =
+            make_double2(S::to_f(dd(vi.hi.lo(), vi.lo.lo()), p.wf[i]), S::to_f(dd(vi.hi.hi(), vi.lo.hi()), p.wf[i]));
       }
     }
   }
