@@ -568,8 +568,8 @@ def main():
 
     e2e = None
     if not args.profile:
-        # three complete end-to-end sequences, the median reported: the host link is shared with
-        # the machine's other GPUs, so a single sequence can catch a neighbour's transfers
+        # three complete end-to-end sequences, the median reported: a single sequence has been
+        # seen to take twice as long as the next two (a transient on the host link)
         runs = [time_e2e(torch, lbm, problem, model, f0, args.steps, dt) for _ in range(3)]
         e2e_runs = [max_over_ranks(r[0], world, "cuda") for r in runs]
         e2e_s, h2d, d2h = sorted(e2e_runs)[1], runs[0][1], runs[0][2]
