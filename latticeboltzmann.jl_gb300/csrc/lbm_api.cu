@@ -641,7 +641,7 @@ int32_t lbm_create(lbm_ctx** out, const lbm_desc* d) {
   c->stream = c->own_stream;
   // the reduction scratch (lbm_reduce) is allocated at the first reduction: members of a batch,
   // whose reductions run batched, never need it, and a sweep creates thousands of them
-  c->red_blocks = (int)std::min<int64_t>((c->n + kRedThreads - 1) / kRedThreads, 152 * 4);
+  c->red_blocks = (int)std::min<int64_t>((c->n + kRedThreads - 1) / kRedThreads, kSumBlocks);
   if (d->force_kind == LBM_FORCE_FIELD) {
     if (!dev_malloc(&c->d_force, (size_t)c->n * 2 * sizeof(double)) ||
         cudaMemcpy(c->d_force, d->force_field, (size_t)c->n * 2 * sizeof(double), cudaMemcpyHostToDevice) !=
@@ -1915,7 +1915,7 @@ int32_t lbm_adjoint_create(lbm_adjoint** out, lbm_ctx* c, int64_t nsteps, int64_
     a->forward_steps = pl.fwd;
   }
   a->bytes = (size_t)c->n * c->Q * c->elem;
-  a->nblocks = (int)std::min<int64_t>((c->n + kAdjThreads - 1) / kAdjThreads, 152 * 4);
+  a->nblocks = (int)std::min<int64_t>((c->n + kAdjThreads - 1) / kAdjThreads, kSumBlocks);
   bool ok = dev_malloc(&a->a0, a->bytes) && dev_malloc(&a->work[0], a->bytes) &&
             dev_malloc(&a->work[1], a->bytes) && dev_malloc(&a->lam[0], a->bytes) &&
             dev_malloc(&a->lam[1], a->bytes) &&

@@ -27,7 +27,7 @@
 
 namespace {
 
-constexpr int kNoAllocBlocks = 608;  // partial sums: 4 blocks per SM on 152 SMs
+constexpr int kNoAllocBlocks = lbm::kSumBlocks;  // the partition of lbm_reduce: the same bits
 constexpr int kNoAllocSlots = kNoAllocBlocks * lbm::kRedMaxK;
 
 static __device__ __align__(256) double g_noalloc_partial[kNoAllocSlots];

@@ -13,6 +13,10 @@
 namespace lbm {
 
 constexpr int kRedThreads = 256;
+// Blocks of a lattice-wide sum (reductions, the adjoint's parameter sums): a fixed partition, not
+// one derived from the device's SM count, so that a sum's FP64 addition order, and so its bits,
+// are the same on every device; 608 is four blocks per SM of a 152-SM GB300.
+constexpr int kSumBlocks = 608;
 constexpr int kRedMaxK = 16;
 
 struct ReduceArgs {
