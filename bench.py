@@ -258,9 +258,9 @@ def bench_mrt_d2q37(torch, lbm, steps=500, n=2048):
     pk = peaks()
     peak = pk["hbm_gbs"] if pk else 6800.0
     out = {"workload": f"D2Q37 regularised MRT shear wave {n}x{n}, tau=0.6, {steps} steps"}
-    for storage, esize in (("f64", 8), ("df64dev", 8), ("f32dev", 4)):
+    for storage, esize in (("f64", 8), ("df64dev", 8), ("f32dev", 4), ("f64dd", 8), ("f32sr", 4)):
         m = lbm.LatticeBoltzmannModel(problem, q, collision_model=lbm.MRT(q, tau), storage=storage, f0=f0)
-        st = steps if storage != "f64" else max(20, steps // 10)
+        st = steps if storage not in ("f64", "f64dd") else max(20, steps // (10 if storage == "f64" else 4))
         sec, _ = time_device(torch, m, st, 3, 1.0)
         row = lbm.track_errors(m, problem, st + 3)
         m.close()

@@ -692,6 +692,11 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
                                                        const typename S::T* __restrict__ src,
                                                        typename S::T* __restrict__ dst) {
   using CT = typename S::C;
+  // FP64-DD MRT: per-thread staging slots, one per population (a float-float pair has the 8 bytes
+  // of the double it replaces; no thread reads another's slots, so no barrier): the double <->
+  // float-float conversions run in loops instead of being inlined Q times each
+  constexpr bool kStage = S::WIDE && COLL == LBM_MRT && MODE != 2;
+  __shared__ double stage[kStage ? L::Q : 1][kStage ? kBlockX : 1];
   wait_prior_grid();
   const int x = blockIdx.x * kBlockX + threadIdx.x;
   if (x >= p.nx) return;
@@ -704,7 +709,49 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
       const bool has_force = p.force_kind != LBM_FORCE_NONE;
       if (has_force) node_shifted_force(p, x, y, sFx, sFy, [&] { return step_time(p); });
       auto out = [&](int i, CT val) { store_out<S>(p, dst, i, node, val); };
-      if constexpr (MODE == 0) {
+      if constexpr (kStage) {
+        int xw[2 * L::R + 1], yo[2 * L::R + 1];
+        bool staged = true;
+        if constexpr (MODE == 0) {
+          static_for<0, L::Q>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            stage[i][threadIdx.x] = src[plane_off(p, i) + node];
+          });
+        } else {
+          pull_offsets<L>(p, x, y, xw, yo);
+          staged = !(p.nbc > 0 && (y < L::R || y >= p.ny - L::R || x < L::R || x >= p.nx - L::R));
+          if (staged)
+            static_for<0, L::Q>([&](auto I) {
+              constexpr int i = decltype(I)::value;
+              stage[i][threadIdx.x] = src[plane_off(p, i) + yo[L::R + L::cy(i)] + xw[L::R + L::cx(i)]];
+            });
+        }
+        if (staged) {
+#pragma unroll 1
+          for (int i = 0; i < L::Q; ++i) {
+            const CT g = S::from_f(stage[i][threadIdx.x], p.wf[i]);
+            stage[i][threadIdx.x] = __hiloint2double(__float_as_int(g.hi), __float_as_int(g.lo));
+          }
+          mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
+                              [&](auto I) {
+                                const double b = stage[decltype(I)::value][threadIdx.x];
+                                return CT(__int_as_float(__double2hiint(b)), __int_as_float(__double2loint(b)));
+                              },
+                              [&](int i, CT val) {
+                                stage[i][threadIdx.x] = __hiloint2double(__float_as_int(val.hi), __float_as_int(val.lo));
+                              });
+#pragma unroll 1
+          for (int i = 0; i < L::Q; ++i) {
+            const double b = stage[i][threadIdx.x];
+            dst[plane_off(p, i) + node] =
+                S::to_f(CT(__int_as_float(__double2hiint(b)), __int_as_float(__double2loint(b))), p.wf[i]);
+          }
+        } else {  // nodes within R of a wall: the pull with its boundary rules, conversions inline
+          mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
+                              [&](auto I) { return pop_streamed<L, S>(p, src, x, y, xw, yo, true, decltype(I)::value); },
+                              out);
+        }
+      } else if constexpr (MODE == 0) {
         mrt_node<L, S::DEV>(p, sFx, sFy, has_force,
                             [&](auto I) {
                               constexpr int i = decltype(I)::value;
