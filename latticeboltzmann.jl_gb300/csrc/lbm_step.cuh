@@ -794,10 +794,11 @@ __global__ void __launch_bounds__(kBlockX, (COLL == LBM_MRT && (S::id == LBM_STO
 // loaded, and all outputs stored, as one aligned two-node access; away from the x edges the
 // second node's addresses are the first's plus one element.  Nodes within R of an x edge, or of
 // a y edge when boundary conditions are set, are pulled by load_streamed.  Needs nx even.
-// Residency: FP16 D2Q4-D2Q9 ten blocks per SM (48 registers), F64DD seven (72 registers, a few
-// spilled words: 20.9 against 20.5 GLUPS at six blocks, D2Q9 4096^2).
+// Residency: FP16 D2Q4-D2Q9 ten blocks per SM (48 registers), F64DD and FP32-SR seven (72
+// registers, a few spilled words; D2Q9 4096^2: F64DD 20.9 against 20.5 GLUPS at six blocks,
+// FP32-SR 41.2 against 40.7 at six and 39.2 at the compiler's 94 registers).
 template <class L, class S>
-__global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <= 9) ? 10 : (S::id == LBM_STORE_F64_DD ? 7 : 0)) step_pair_kernel(StepParams<typename S::C> p,
+__global__ void __launch_bounds__(kBlockX, (S::id == LBM_STORE_F16_DEV && L::Q <= 9) ? 10 : (S::id == LBM_STORE_F64_DD || S::id == LBM_STORE_F32_DEV_SR ? 7 : 0)) step_pair_kernel(StepParams<typename S::C> p,
                                                             const typename S::T* __restrict__ src,
                                                             typename S::T* __restrict__ dst) {
   using T = typename S::T;
